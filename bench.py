@@ -1,0 +1,386 @@
+"""Octree-build benchmark (one JSON line on rank 0).
+
+Workload (default): the 16,777,216-point uniform cloud in [0,1024)^3 of seed
+114514 (the reference's k_InitRandomVec4 stream), all eight stages: Morton
+encode, radix sort, unique, Karras radix tree, edge count, prefix sum, octree
+nodes and leaf links. One step = one whole build of that cloud.
+
+  value  Mpoints/s with the points already resident in HBM, timed with CUDA
+         events around each step (L2 flushed between steps; the 256 MiB input
+         is also larger than L2);
+  e2e    the same metric through the C ABI call a user makes, with the step's
+         points copied host->device from pinned memory and the octree
+         (M OctNodes + counts) copied back inside the timed region;
+  roofline  the dominant kernel's algorithmic bytes per launch over its
+         average duration (CUDA events recorded by oct_build_octree_timed on
+         the launching stream), against MEASURED_PEAKS.json's HBM copy rate;
+  cpu_baseline  the CPU port of the reference pipeline (oracle/oracle.c,
+         OpenMP on all host cores) timed on the same cloud.
+
+--impl reference times that CPU implementation alone (the reference's own
+sources cannot be built on the GPU host; the restatement is pinned to them
+byte for byte by tests/test_oracle_golden.py).
+
+Multi-GPU: one process per GPU (torchrun). A single cloud does not shard, so
+N ranks build N independent replicas (weak scaling); value = all points built
+by all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpoints/s octree build, learned+batched vs plain GPU (bit-exact); % HBM peak"
+UNIT = "Mpoints/s"
+N_POINTS = 1 << 24
+SEED = 114514
+MIN_COORD, RANGE = 0.0, 1024.0
+WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 114514 "
+            "(k_InitRandomVec4 stream), 30-bit Morton, all stages Morton..leaf links")
+
+# Algorithmic bytes per kernel launch of the build (per point / node / slot),
+# as fixed by the octree-build analysis: stage 1 reads 16 B and writes 4 B per
+# point (its digit histograms are fused, so the sort reads no extra 4 B/key);
+# each 10-bit sort pass reads and writes 4 B per key; unique reads 4 B per key
+# and writes 4 B per unique key; the radix tree reads 4 B per code and writes
+# 11 B per node; edge count + prefix sum read 1+4+1 B and write 4+4 B per
+# node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
+# leaf link (split over the emit and finalize launches).
+def algorithmic_bytes(n, u, b, m):
+    leaves = b + 1
+    return {
+        "morton+histogram": 20 * n,
+        "sort pass 0": 8 * n,
+        "sort pass 1": 8 * n,
+        "sort pass 2": 8 * n,
+        "unique": 4 * n + 4 * u,
+        "radix tree": 4 * u + 11 * b,
+        "edge count+prefix sum": 14 * b,
+        "octree emit": 40 * b + 4 * leaves,
+        "octree finalize": 60 * m,
+    }
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_points(n):
+    from pipeline_gb300.kernels import k_InitRandomVec4
+
+    return k_InitRandomVec4(None, n, MIN_COORD, RANGE, SEED)
+
+
+# ----------------------------------------------------------------- CPU side --
+def cpu_build_time(pts, threads, reps):
+    """Seconds per whole CPU build (stages 1-8, OpenMP as the reference)."""
+    from oracle import oracle as O
+
+    times = []
+    for _ in range(reps):
+        r = O.build_all(pts, MIN_COORD, RANGE, threads=threads, parallel_octree=threads > 1,
+                        keep_morton=False)
+        times.append(float(np.sum(r["stage_ms"])) / 1e3)
+    return times, r
+
+
+def cpu_baseline(pts, reps=2):
+    from oracle import oracle as O
+
+    threads = O.lib().orc_max_threads()
+    times, _ = cpu_build_time(pts, threads, reps)
+    t = statistics.median(times)
+    return {"value": len(pts) / t / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} whole builds of the 16,777,216-point cloud, median "
+                      f"{t * 1e3:.0f} ms each (stages 1-8; octree stage multi-threaded as in the "
+                      f"reference)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    pts = make_points(N_POINTS)
+    threads = O.lib().orc_max_threads()
+    cpu_build_time(pts, threads, max(args.warmup, 0))
+    times, _ = cpu_build_time(pts, threads, args.steps)
+    total = float(sum(times))
+    value = N_POINTS * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "n_points": N_POINTS},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} whole builds of the workload (after "
+                                   f"{args.warmup} warm-up builds) on {threads} host threads; "
+                                   "the reference's sources do not build on the GPU host, the "
+                                   "timed code is their byte-identical C restatement"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- GPU side --
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from pipeline_gb300 import _lib
+    from pipeline_gb300.pipeline import OctreeBuilder
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    lib = _lib.load()
+    pts_h = make_points(N_POINTS)
+    pts = torch.from_numpy(pts_h).to(dev)
+    builder = OctreeBuilder(N_POINTS, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    # L2 flush buffer (larger than the 129 MB L2).
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    # warm-up (also records the sizes)
+    for _ in range(max(args.warmup, 3)):
+        builder.build(pts, MIN_COORD, RANGE)
+    counts = builder.counts()
+    if counts.status != 0:
+        raise RuntimeError(f"device status {counts.status}")
+    n, u, b, m = N_POINTS, counts.n_unique, counts.n_brt, counts.n_oct
+
+    # ---- device-resident timing (value) ----
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local_rank)
+    barrier()
+    sampler.start()
+    time.sleep(0.25)
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        builder.build(pts, MIN_COORD, RANGE)
+        ends[k].record(stream)
+    barrier()
+    t_wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world / (ms / 1e3) / 1e6
+
+    # ---- per-kernel times (timed build, events on the launching stream) ----
+    nsteps = lib.oct_build_step_count()
+    names = [lib.oct_build_step_name(i).decode() for i in range(nsteps)]
+    reps = max(3, min(args.steps, 10))
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(nsteps)] for _ in range(reps)]
+    for r in range(reps):
+        flush.fill_(r & 0xFF)
+        handles = (C.c_void_p * nsteps)(*[e.cuda_event for e in evs[r]])
+        rc = lib.oct_build_octree_timed(C.c_void_p(pts.data_ptr()), n, MIN_COORD, RANGE,
+                                        C.byref(builder._out), C.c_void_p(builder.workspace.data_ptr()),
+                                        builder.workspace.numel(), handles, nsteps,
+                                        C.c_void_p(stream.cuda_stream))
+        _lib.check(rc, "oct_build_octree_timed")
+    torch.cuda.synchronize(dev)
+    per_kernel = {}
+    for i in range(1, nsteps):
+        per_kernel[names[i]] = statistics.median(evs[r][i - 1].elapsed_time(evs[r][i]) for r in range(reps))
+    alg = algorithmic_bytes(n, u, b, m)
+    hbm_peak, peak_kind = peaks()
+    stages = {}
+    for name, t in per_kernel.items():
+        entry = {"ms": round(t, 4)}
+        if name in alg and t > 0:
+            gbs = alg[name] / (t / 1e3) / 1e9
+            entry.update(gbs=round(gbs, 1), frac=round(gbs / hbm_peak, 3))
+        stages[name] = entry
+    dom = max((k for k in per_kernel if k in alg), key=lambda k: per_kernel[k])
+    dom_gbs = alg[dom] / (per_kernel[dom] / 1e3) / 1e9
+    traffic = read_traffic(dom, n)
+    total_alg = sum(alg.values())
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": hbm_peak,
+                "unit": "GB/s", "frac": round(dom_gbs / hbm_peak, 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                else "fallback 6800 GB/s",
+                "end_to_end_frac": round(total_alg / (ms / 1e3) / 1e9 / hbm_peak, 4),
+                "algorithmic_bytes_per_step": int(total_alg)}
+
+    # ---- end to end through the C ABI with host buffers (e2e) ----
+    pinned = torch.from_numpy(pts_h).pin_memory()
+    nodes_h = torch.empty((m, 15), dtype=torch.int32).pin_memory()
+    counts_h = torch.empty(4, dtype=torch.int32).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    es = [torch.cuda.Event(enable_timing=True) for _ in range(e2e_steps)]
+    ee = [torch.cuda.Event(enable_timing=True) for _ in range(e2e_steps)]
+    barrier()
+    for k in range(e2e_steps):
+        flush.fill_(k & 0xFF)
+        es[k].record(stream)
+        pts.copy_(pinned, non_blocking=True)
+        builder.build(pts, MIN_COORD, RANGE)
+        counts_h.copy_(builder.d_counts, non_blocking=True)
+        nodes_h.copy_(builder.nodes[:m], non_blocking=True)
+        ee[k].record(stream)
+    barrier()
+    e2e_ms = statistics.mean(s.elapsed_time(e) for s, e in zip(es, ee))
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    assert int(counts_h[2]) == m
+    e2e = {"value": n * world / (e2e_ms / 1e3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+           "d2h_bytes_per_step": m * 60 + 16, "ms_per_step": round(e2e_ms, 4)}
+
+    if rank != 0:
+        return 0
+    base = None
+    if world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(pts_h)
+    launches_per_step = nsteps - 2  # every step but "start" and the memset "clear"
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_points": n, "n_unique": u, "n_oct_nodes": m,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed between steps (256 MiB write); input 256 MiB > L2",
+                   "wall_s_timed_region": round(t_wall, 3)},
+        "roofline": roofline, "stages": stages, "e2e": e2e,
+        "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+        "cpu_baseline": base,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def read_traffic(kernel_step: str, n: int):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/dram_traffic.txt: '<step name>|<bytes per launch>|<n>'),
+    scaled to n points; None when no capture covers it."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for ln in f:
+            parts = ln.strip().split("|")
+            if len(parts) == 3 and parts[0] == kernel_step:
+                return int(float(parts[1]) * n / float(parts[2]))
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    try:
+        return run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,247 @@
+/*
+ * octree_gb300.h — C ABI of the GB300 (sm_103a) octree-build library
+ * (libpipeline_gb300.so).
+ *
+ * Drop-in for the seven-stage octree build of ucsc-redwood/pipeline: Morton
+ * encode, radix sort, unique, Karras radix tree, edge count, prefix sum and
+ * octree nodes (+ leaf links). Each stage entry point below names the
+ * reference function it replaces (paths within the reference project).
+ *
+ * Conventions
+ *  - Plain C: pointers, sizes, a CUDA stream (may be NULL = legacy stream).
+ *  - Pointers are DEVICE pointers (cudaMalloc / cudaMallocManaged) unless a
+ *    function says otherwise. The caller owns every buffer, as in the
+ *    reference (include/shared/types.h:5-8).
+ *  - Entry points are asynchronous on the given stream and return an
+ *    oct_status for argument / launch errors. Conditions found on the device
+ *    (a look-back wait that ran out its bound, a coordinate outside
+ *    [min, min + range], a too-small octree capacity) are OR-ed into an
+ *    optional device status word (OCT_STATUS_* bits); no call aborts or traps.
+ *  - Scratch comes from a caller workspace whose size the matching
+ *    *_workspace_bytes() function returns (256-byte aligned base required).
+ *  - Results are bit-identical to the reference's CPU implementation on the
+ *    same inputs, run with one thread, under these conventions where the
+ *    reference leaves behaviour undefined:
+ *      O1  the radix tree has n_nodes = U - 1 nodes (apps/cpu_demo/main.cpp:95);
+ *      O3  the octree has M = 1 + the largest slot stages 7-8 write
+ *          (= prefix_sum[U-2] + 1 whenever the reference stays in bounds);
+ *      O4  outputs start zeroed (OctNodes, parent[]);
+ *      O6  stages 7-8 take the values a sequential ascending-node run leaves;
+ *      O7  a leaf-link walk stops at radix node 0 (the reference never returns);
+ *      O10 a shift by a negative count (leaf level 11) shifts by count mod 32;
+ *      O11 a one-node tree (U = 2) uses clz(0) = 32 and drops the
+ *          out-of-range parent write.
+ */
+#ifndef OCTREE_GB300_H
+#define OCTREE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define OCT_API __attribute__((visibility("default")))
+#else
+#define OCT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without including the CUDA headers. */
+typedef struct CUstream_st* oct_stream_t;
+
+/* glm::vec4 as the reference stores points and corners: four floats, 16 B. */
+typedef struct oct_vec4 {
+  float x, y, z, w;
+} oct_vec4;
+
+/* OctNode (reference include/shared/types.h:28-34), 60 bytes. */
+typedef struct oct_node {
+  int32_t children[8];
+  oct_vec4 corner;
+  float cell_size;
+  int32_t child_node_mask;
+  int32_t child_leaf_mask;
+} oct_node;
+
+/* RadixTreeData (reference include/shared/types.h:14-21); bool is 1 byte. */
+typedef struct oct_radix_tree {
+  int32_t n_nodes;
+  uint8_t* prefix_n;
+  uint8_t* has_leaf_left;
+  uint8_t* has_leaf_right;
+  int32_t* left_child;
+  int32_t* parent;
+} oct_radix_tree;
+
+typedef enum oct_status {
+  OCT_OK = 0,
+  OCT_ERR_INVALID_ARG = 1, /* bad size, null pointer, misaligned buffer */
+  OCT_ERR_WORKSPACE = 2,   /* workspace smaller than *_workspace_bytes() */
+  OCT_ERR_CUDA = 3,        /* a CUDA runtime call or launch failed */
+  OCT_ERR_DEVICE = 4,      /* the device status word is non-zero (sync calls) */
+  OCT_ERR_CAPACITY = 5     /* octree node buffer too small (sync calls) */
+} oct_status;
+
+/* Device status word bits. */
+#define OCT_STATUS_SPIN_TIMEOUT 1u /* a decoupled look-back wait gave up */
+#define OCT_STATUS_WALK_LIMIT 2u   /* a radix-tree parent walk exceeded 64 steps */
+#define OCT_STATUS_RANGE 4u        /* a coordinate outside [min, min + range] or NaN */
+#define OCT_STATUS_CAPACITY 8u     /* octree needs more nodes than the buffer holds */
+
+/* Largest point / key count accepted (counts travel in 30-bit fields). */
+#define OCT_MAX_N ((1 << 30) - 1)
+
+/* Library version and the device architecture it was built for (e.g. 1033 = sm_103a). */
+OCT_API int oct_version(void);
+OCT_API int oct_built_arch(void);
+/* Last CUDA error string seen by the library on this thread ("" if none). */
+OCT_API const char* oct_last_error(void);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 0 (host): input generator. Replaces k_InitRandomVec4               */
+/* (include/kernels/00_init.hpp:10-11): n points drawn from std::mt19937     */
+/* (seed) through std::uniform_real_distribution<float>(min, min + range),   */
+/* z drawn first, then y, then x (GCC's argument order); w = 1. `out` is a   */
+/* HOST pointer.                                                             */
+/* ----------------------------------------------------------------------- */
+OCT_API void oct_init_random_vec4(oct_vec4* out, int n, float min_coord, float range, int seed);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 1: Morton encode. Replaces k_ComputeMortonCode                     */
+/* (include/kernels/01_morton.hpp:9-13; GPU kernels/cuda/01_morton.cu:8-19).*/
+/* keys[i] = 30-bit Morton code of points[i] (w ignored).                   */
+/* ----------------------------------------------------------------------- */
+OCT_API int oct_morton_encode(const oct_vec4* points, uint32_t* keys, int64_t n, float min_coord,
+                      float range, uint32_t* d_status, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 2: sort keys ascending, in place. Replaces k_SimpleRadixSort       */
+/* (include/kernels/02_sort.hpp:6-7) and the GPU OneSweep dispatch          */
+/* (apps/gpu_demo/main.cu:63-125). key_bits: significant low bits of every  */
+/* key (30 for Morton codes, 32 for arbitrary keys). keys_alt: n-entry      */
+/* scratch (the reference's keys_alt / OneSweepData::u_sort_alt).           */
+/* ----------------------------------------------------------------------- */
+OCT_API size_t oct_sort_workspace_bytes(int n, int key_bits);
+OCT_API int oct_sort_keys(uint32_t* keys, uint32_t* keys_alt, int n, int key_bits, void* workspace,
+                  size_t workspace_bytes, uint32_t* d_status, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 3: unique. Replaces k_CountUnique (include/kernels/03_unique.hpp:4,*/
+/* kernels/03_unique.cpp:2-16): compacts runs of equal keys in place and    */
+/* writes U to *d_n_unique (device int). keys[U, n) keep their old values.  */
+/* ----------------------------------------------------------------------- */
+OCT_API size_t oct_unique_workspace_bytes(int n);
+OCT_API int oct_unique(uint32_t* keys, int n, int32_t* d_n_unique, void* workspace, size_t workspace_bytes,
+               uint32_t* d_status, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 4: Karras radix tree over codes[0..n_nodes]. Replaces              */
+/* k_BuildRadixTree (include/kernels/04_radix_tree.hpp:5-11). n_nodes is    */
+/* U - 1. parent[] entries no node writes (parent[0], and parent[n-1] when  */
+/* the root spans one key short) are set to 0.                              */
+/* ----------------------------------------------------------------------- */
+OCT_API int oct_build_radix_tree(int n_nodes, const uint32_t* codes, uint8_t* prefix_n,
+                         uint8_t* has_leaf_left, uint8_t* has_leaf_right, int32_t* left_child,
+                         int32_t* parent, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 5: edge count. Replaces k_EdgeCount                                 */
+/* (include/kernels/05_edge_count.hpp:5-8): ec[0] = 0,                       */
+/* ec[i] = prefix_n[i]/3 - prefix_n[parent[i]]/3.                            */
+/* ----------------------------------------------------------------------- */
+OCT_API int oct_edge_count(const uint8_t* prefix_n, const int32_t* parent, int32_t* edge_count,
+                   int n_nodes, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 6: inclusive prefix sum. Replaces k_PartialSum                      */
+/* (include/kernels/06_partial_sum.hpp:6-9) over data[0, n).                 */
+/* ----------------------------------------------------------------------- */
+OCT_API size_t oct_prefix_sum_workspace_bytes(int n);
+OCT_API int oct_prefix_sum(const int32_t* data, int n, int32_t* out, void* workspace,
+                   size_t workspace_bytes, uint32_t* d_status, oct_stream_t stream);
+
+/* Number of octree nodes stages 7-8 need for this tree (O3): one past the
+ * largest slot they write. Asynchronous: writes the count to the device int
+ * *n_oct_nodes on the stream (the host reads it after the stream drains, as
+ * apps/cpu_demo/main.cpp:120 reads num_oct_nodes). */
+OCT_API int oct_octree_node_count(const int32_t* edge_count, const int32_t* prefix_sum,
+                                  int n_nodes, int32_t* n_oct_nodes, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 7: octree nodes. Replaces k_MakeOctNodes                            */
+/* (include/kernels/07_octree.hpp:5-14, shared/oct.h:24-90). Applies the     */
+/* writes of radix nodes 1..n_nodes-1 to nodes[0, n_oct_nodes) in the order  */
+/* a one-thread reference run makes them; the caller initialises nodes      */
+/* (zeroed, root at slot 0) as apps/cpu_demo/main.cpp:123-132 does, or uses  */
+/* oct_octree_root_init.                                                     */
+/* ----------------------------------------------------------------------- */
+OCT_API size_t oct_octree_workspace_bytes(int n_oct_nodes);
+OCT_API int oct_octree_root_init(oct_node* nodes, const uint32_t* codes, const uint8_t* prefix_n,
+                         float min_coord, float range, oct_stream_t stream);
+OCT_API int oct_make_oct_nodes(oct_node* nodes, int n_oct_nodes, const int32_t* node_offsets,
+                       const int32_t* rt_node_counts, const uint32_t* codes,
+                       const uint8_t* rt_prefix_n, const int32_t* rt_parents, float min_coord,
+                       float range, int n_nodes, void* workspace, size_t workspace_bytes,
+                       uint32_t* d_status, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Stage 8: leaf links. Replaces k_LinkLeafNodes                             */
+/* (include/kernels/07_octree.hpp:16-25, shared/oct.h:92-134).               */
+/* ----------------------------------------------------------------------- */
+OCT_API int oct_link_leaf_nodes(oct_node* nodes, int n_oct_nodes, const int32_t* node_offsets,
+                        const int32_t* rt_node_counts, const uint32_t* codes,
+                        const uint8_t* rt_has_leaf_left, const uint8_t* rt_has_leaf_right,
+                        const uint8_t* rt_prefix_n, const int32_t* rt_parents,
+                        const int32_t* rt_left_child, int n_nodes, void* workspace,
+                        size_t workspace_bytes, uint32_t* d_status, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Whole build: stages 1-8 in the order of apps/cpu_demo/main.cpp:72-154,    */
+/* all sizes kept on the device (no host round trip, CUDA-graph capturable). */
+/* Outputs (device, caller-owned; n = number of points):                     */
+/*   codes            uint32[n]  sorted unique Morton codes (first U valid)   */
+/*   tree             arrays of >= n entries (first U - 1 valid)              */
+/*   edge_count, prefix_sum  int32[n] (first U - 1 valid)                     */
+/*   nodes            oct_node[nodes_capacity] (first M valid)                */
+/*   d_counts         int32[4] = {U, U - 1, M, status bits}                   */
+/* When M > nodes_capacity the octree stage is skipped and status carries    */
+/* OCT_STATUS_CAPACITY; d_counts[2] still reports the M needed.              */
+/* ----------------------------------------------------------------------- */
+typedef struct oct_build_outputs {
+  uint32_t* codes;
+  oct_radix_tree tree;
+  int32_t* edge_count;
+  int32_t* prefix_sum;
+  oct_node* nodes;
+  int32_t nodes_capacity;
+  int32_t* d_counts;
+} oct_build_outputs;
+
+OCT_API size_t oct_build_workspace_bytes(int n, int nodes_capacity);
+OCT_API int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range,
+                     const oct_build_outputs* out, void* workspace, size_t workspace_bytes,
+                     oct_stream_t stream);
+
+/* Timed build for measurement: the same launches as oct_build_octree, with
+ * caller-created CUDA events (cudaEvent_t, passed as void*) recorded on the
+ * stream at each step boundary: events[k] after step k of
+ * oct_build_step_name(k) for k < oct_build_step_count() (step 0 is the start).
+ * Bench tooling derives per-kernel device times from consecutive events. */
+OCT_API int oct_build_step_count(void);
+OCT_API const char* oct_build_step_name(int k);
+OCT_API int oct_build_octree_timed(const oct_vec4* points, int n, float min_coord, float range,
+                                   const oct_build_outputs* out, void* workspace,
+                                   size_t workspace_bytes, void* const* events, int n_events,
+                                   oct_stream_t stream);
+
+/* Synchronous convenience: copies d_counts to the host after the stream
+ * drains and maps the status word to OCT_ERR_DEVICE / OCT_ERR_CAPACITY. */
+OCT_API int oct_read_counts(const int32_t* d_counts, int32_t* h_counts, oct_stream_t stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* OCTREE_GB300_H */

@@ -1,0 +1,161 @@
+// Shared device helpers for the sm_103a octree-build kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace octgb {
+
+// Device status word bits (mirrored by OCT_STATUS_* in include/octree_gb300.h).
+constexpr uint32_t kStatusSpinTimeout = 1u;  // a look-back wait ran out its bound
+constexpr uint32_t kStatusWalkLimit = 2u;    // a parent walk exceeded its bound
+constexpr uint32_t kStatusRange = 4u;        // a coordinate outside [min, min + range]
+constexpr uint32_t kStatusCapacity = 8u;     // octree node capacity too small
+
+// A look-back poll costs an L2 round trip plus a 64 ns sleep after the first
+// few misses, so this bound ends a wait that never completes in about a second.
+constexpr uint32_t kSpinLimit = 1u << 21;
+
+constexpr int kWarp = 32;
+
+__device__ __forceinline__ uint32_t lane_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Streaming (evict-first) 128-bit load for data read exactly once.
+__device__ __forceinline__ float4 ld_stream_f4(const float4* p) {
+  float4 v;
+  asm volatile("ld.global.cs.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ void backoff(uint32_t it) {
+  if (it > 8) __nanosleep(64);
+}
+
+__device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bit) {
+  if (status) atomicOr(status, bit);
+}
+
+// Karras-tree helpers with the reference's integer semantics
+// (kernels/04_radix_tree.cpp:16-37): delta is clz(a ^ b) - 1 stored in a
+// uint8_t (so keys differing in bit 31 give 255); clz(0) is 32.
+__device__ __forceinline__ int delta_u8(uint32_t a, uint32_t b) {
+  return (int)(uint8_t)(__clz(a ^ b) - 1);
+}
+
+__device__ __forceinline__ int log2_ceil_u32(uint32_t x) {
+  const int fl = 31 - __clz(x);
+  return fl + ((1u << fl) < x);
+}
+
+// Morton helpers (include/shared/morton.h:15-80), restated.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  uint32_t x = v & 0x3ffu;
+  x = (x | (x << 16)) & 0x030000ffu;
+  x = (x | (x << 8)) & 0x0300f00fu;
+  x = (x | (x << 4)) & 0x030c30c3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t compact3(uint32_t m) {
+  uint32_t x = m & 0x09249249u;
+  x = (x ^ (x >> 2)) & 0x030c30c3u;
+  x = (x ^ (x >> 4)) & 0x0300f00fu;
+  x = (x ^ (x >> 8)) & 0x030000ffu;
+  x = (x ^ (x >> 16)) & 0x000003ffu;
+  return x;
+}
+
+// FP32 quantisation in the reference's operation order, each step rounded to
+// nearest with no contraction: (v - min) / range * 1024, truncated.
+__device__ __forceinline__ uint32_t quantise(float v, float min_coord, float range) {
+  const float q = __fmul_rn(__fdiv_rn(__fsub_rn(v, min_coord), range), 1024.0f);
+  return __float2uint_rz(q);
+}
+
+__device__ __forceinline__ bool in_range(float v, float min_coord, float range) {
+  // Outside [min, min + range] (or NaN) is undefined behaviour in the
+  // reference's float-to-uint cast; flag it.
+  const float q = __fmul_rn(__fdiv_rn(__fsub_rn(v, min_coord), range), 1024.0f);
+  return q >= 0.0f && q <= 1024.0f;
+}
+
+__device__ __forceinline__ uint32_t morton_code(float x, float y, float z, float min_coord,
+                                                float range) {
+  return spread3(quantise(x, min_coord, range)) | (spread3(quantise(y, min_coord, range)) << 1) |
+         (spread3(quantise(z, min_coord, range)) << 2);
+}
+
+// morton32_to_xyz: per axis (raw / 1024) * range + min, w = 1.
+__device__ __forceinline__ float4 decode_corner(uint32_t code, float min_coord, float range) {
+  float4 c;
+  c.x = __fadd_rn(__fmul_rn(__fdiv_rn((float)compact3(code), 1024.0f), range), min_coord);
+  c.y = __fadd_rn(__fmul_rn(__fdiv_rn((float)compact3(code >> 1), 1024.0f), range), min_coord);
+  c.z = __fadd_rn(__fmul_rn(__fdiv_rn((float)compact3(code >> 2), 1024.0f), range), min_coord);
+  c.w = 1.0f;
+  return c;
+}
+
+// Block-wide exclusive sum of one value per thread (THREADS a multiple of 32).
+template <int THREADS, typename T>
+__device__ __forceinline__ T block_exclusive_sum(T v, T* warp_tot /* THREADS/32 */, T* total) {
+  constexpr int W = THREADS / kWarp;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    T x = lane < W ? warp_tot[lane] : T(0);
+    T xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += t;
+    }
+    if (lane < W) warp_tot[lane] = xi - x;
+    if (lane == W - 1) *total = xi;
+  }
+  __syncthreads();
+  const T r = warp_tot[w] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+}  // namespace octgb

@@ -1,0 +1,123 @@
+// Internal launch interface shared by the kernel translation units and the
+// C-ABI layer (api.cu). Nothing here is exported from the shared library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "octree_gb300.h"
+
+namespace octgb {
+
+static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Optional per-launch event recording (timed builds): mark() records the next
+// caller event on the stream after a launch.
+struct Recorder {
+  cudaEvent_t* events = nullptr;
+  int n = 0;
+  int k = 0;
+  void mark(cudaStream_t s) {
+    if (k < n) cudaEventRecord(events[k], s);
+    ++k;
+  }
+};
+static inline void mark(Recorder* r, cudaStream_t s) {
+  if (r) r->mark(s);
+}
+
+int device_sm_count();
+
+// ---- sort ----------------------------------------------------------------
+struct SortPlan {
+  int n;
+  int radix_bits;
+  int passes;
+  int bins;
+  int tile;
+  int tiles;
+  size_t hist_off, base_off, counter_off, lookback_off;
+  size_t bytes;  // control block, zeroed before each sort
+};
+
+SortPlan sort_plan(int n, int key_bits);
+
+// Morton encode; with plan != nullptr also accumulates the plan's digit
+// histograms into the zeroed control block ctrl.
+cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float min_coord,
+                          float range, const SortPlan* plan, void* ctrl, uint32_t* status,
+                          cudaStream_t s);
+cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* ctrl,
+                             cudaStream_t s);
+cudaError_t launch_sort_passes(uint32_t* keys, uint32_t* alt, const SortPlan* plan, void* ctrl,
+                               uint32_t* status, cudaStream_t s, uint32_t** result,
+                               Recorder* rec = nullptr);
+
+// ---- unique --------------------------------------------------------------
+struct ScanPlan {
+  int n;
+  int tile;
+  int tiles;
+  size_t counter_off, lookback_off;
+  size_t bytes;  // control block, zeroed before each launch
+};
+ScanPlan unique_plan(int n);
+// Compacts runs of equal keys of src[0, n) into dst (dst == src allowed);
+// writes U to *d_count.
+cudaError_t launch_unique(const uint32_t* src, uint32_t* dst, int n, int* d_count,
+                          const ScanPlan* plan, void* ctrl, uint32_t* status, cudaStream_t s);
+
+// ---- radix tree, edge count, prefix sum -----------------------------------
+// n_nodes from the host (n_host) or, when d_unique != nullptr, as *d_unique - 1.
+cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* codes,
+                              uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
+                              int* parent, cudaStream_t s);
+
+ScanPlan edge_scan_plan(int n);
+enum EdgeScanMode { kEdgeOnly = 1, kScanOnly = 2, kEdgeAndScan = 3 };
+// kEdgeOnly: ec = edge counts. kScanOnly: ps = inclusive scan of ec.
+// kEdgeAndScan: both, fused. With d_max_slot != nullptr, atomically raises
+// *d_max_slot to the largest octree slot stages 7-8 will write.
+cudaError_t launch_edge_scan(int mode, int n_host, const int* d_unique, const uint8_t* prefix_n,
+                             const int* parent, int* ec, int* ps, int* d_max_slot,
+                             const ScanPlan* plan, void* ctrl, uint32_t* status, cudaStream_t s);
+
+// ---- octree --------------------------------------------------------------
+struct OctTags {
+  uint32_t* child;  // [cap * 8] winning write tag per (slot, child)
+  uint32_t* owner;  // [cap] last radix node that wrote corner / cell_size
+  uint32_t* mask;   // [cap] OR of SetChild bits
+  int cap;
+};
+size_t oct_tags_bytes(int cap);
+OctTags oct_tags_carve(void* base, int cap);
+
+enum OctMode { kOctMake = 1, kOctLink = 2, kOctFresh = 4 };
+
+struct OctArgs {
+  oct_node* nodes;
+  int cap;
+  const int* offsets;      // prefix sum
+  const int* counts;       // edge count
+  const uint32_t* codes;   // sorted unique codes
+  const uint8_t* prefix_n;
+  const uint8_t* hll;
+  const uint8_t* hlr;
+  const int* parent;
+  const int* left_child;
+  float min_coord, range;
+  int n_brt_host;          // used when d_unique == nullptr
+  const int* d_unique;     // U on the device (n_brt = U - 1)
+  int n_oct_host;          // used when d_max_slot == nullptr
+  const int* d_max_slot;   // largest slot on the device (n_oct = max_slot + 1)
+};
+cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t* status,
+                          cudaStream_t s, Recorder* rec = nullptr);
+
+// Copies U, B, M, status into out[4] (device).
+cudaError_t launch_publish_counts(const int* d_unique, const int* d_max_slot,
+                                  const uint32_t* status, int* out, cudaStream_t s);
+
+}  // namespace octgb

@@ -1,0 +1,278 @@
+// Stages 7-8: octree nodes and leaf links.
+//
+// Replaces k_MakeOctNodes / k_LinkLeafNodes (reference
+// include/kernels/07_octree.hpp:5-25, include/shared/oct.h:9-134; GPU form
+// kernels/cuda/07_octree.cu:8-67) and the caller's root set-up
+// (apps/cpu_demo/main.cpp:125-132).
+//
+// The reference's node slots come from an inclusive prefix sum, so the slot
+// ranges of consecutive radix nodes overlap and several radix nodes write the
+// same OctNode fields; its parallel loops then race. The contract is the
+// result of a sequential run in ascending radix-node order (LinkLeaf's left
+// write before its right one, all LinkLeaf writes after all MakeOctNodes
+// writes). The GPU reproduces it without ordering threads:
+//
+//   emit      one thread per radix node computes every write it would make
+//             and records, per (slot, child), the largest sequence tag
+//             (atomicMax), per slot the largest writer of corner/cell_size,
+//             and ORs child_node_mask bits;
+//   finalize  one thread per slot turns the winning tags back into values
+//             (a tag names its radix node and step) and writes the 60-byte
+//             node once, coalesced.
+//
+// Sequence tags (32-bit, larger = later):
+//   MakeOctNodes step j of node i : ((i << 4) | j) + 1        (i < 2^27)
+//   LinkLeafNodes side s of node i: 0x80000000 | (i << 1) | s
+#include "kernels.cuh"
+
+namespace octgb {
+
+constexpr uint32_t kLinkTag = 0x80000000u;
+
+size_t oct_tags_bytes(int cap) {
+  const size_t c = cap > 0 ? (size_t)cap : 1;
+  return align_up(c * 8 * 4, 256) + align_up(c * 4, 256) * 2;
+}
+
+OctTags oct_tags_carve(void* base, int cap) {
+  const size_t c = cap > 0 ? (size_t)cap : 1;
+  char* p = static_cast<char*>(base);
+  OctTags t;
+  t.child = reinterpret_cast<uint32_t*>(p);
+  p += align_up(c * 8 * 4, 256);
+  t.owner = reinterpret_cast<uint32_t*>(p);
+  p += align_up(c * 4, 256);
+  t.mask = reinterpret_cast<uint32_t*>(p);
+  t.cap = cap;
+  return t;
+}
+
+struct Sizes {
+  int n_brt, n_oct;
+  bool fits;
+};
+
+__device__ __forceinline__ Sizes read_sizes(const OctArgs& a) {
+  Sizes z;
+  z.n_brt = a.d_unique ? max(*a.d_unique - 1, 0) : a.n_brt_host;
+  if (a.d_max_slot)
+    z.n_oct = z.n_brt >= 1 ? *a.d_max_slot + 1 : 0;
+  else
+    z.n_oct = a.n_oct_host;
+  z.fits = z.n_oct <= a.cap;
+  return z;
+}
+
+__global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
+                                                       uint32_t* __restrict__ status) {
+  const Sizes z = read_sizes(a);
+  if (!z.fits) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, kStatusCapacity);
+    return;
+  }
+  const int stride = gridDim.x * blockDim.x;
+  uint4* c4 = reinterpret_cast<uint4*>(t.child);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < z.n_oct; p += stride) {
+    c4[2 * p] = make_uint4(0, 0, 0, 0);
+    c4[2 * p + 1] = make_uint4(0, 0, 0, 0);
+    t.owner[p] = 0;
+    t.mask[p] = 0;
+  }
+}
+
+__device__ __forceinline__ void put_child(const OctTags& t, int slot, int which, uint32_t tag,
+                                          int n_oct, uint32_t* status) {
+  if ((unsigned)slot >= (unsigned)n_oct) {
+    raise_status(status, kStatusCapacity);
+    return;
+  }
+  atomicMax(&t.child[(size_t)slot * 8 + which], tag);
+}
+
+__global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctTags t,
+                                                       uint32_t* __restrict__ status) {
+  const Sizes z = read_sizes(a);
+  if (!z.fits) return;
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < z.n_brt; i += stride) {
+    const int L = a.prefix_n[i] / 3;
+    if ((mode & kOctMake) && i >= 1) {
+      // include/shared/oct.h:24-90
+      const int k = a.counts[i];
+      if (k > 0) {
+        const int base = a.offsets[i];
+        const uint32_t code = a.codes[i];
+        for (int j = 0; j < k - 1; ++j) {
+          const int level = L - j;
+          const uint32_t pre = code >> (30 - 3 * level);
+          const int which = (int)(pre & 7u);
+          const int up = base + j + 1;
+          put_child(t, up, which, (((uint32_t)i << 4) | (uint32_t)j) + 1u, z.n_oct, status);
+          if ((unsigned)up < (unsigned)z.n_oct) atomicOr(&t.mask[up], 1u << which);
+          if ((unsigned)(base + j) < (unsigned)z.n_oct) atomicMax(&t.owner[base + j], (uint32_t)i);
+        }
+        int rp = a.parent[i];
+        int counter = 0;
+        bool bad = (unsigned)rp >= (unsigned)z.n_brt;
+        while (!bad && a.counts[rp] == 0) {
+          rp = a.parent[rp];
+          bad = (unsigned)rp >= (unsigned)z.n_brt;
+          if (++counter > 30) break;
+        }
+        if (bad) {  // malformed parent[]: never read out of bounds
+          raise_status(status, kStatusWalkLimit);
+          rp = 0;
+        }
+        const int top = L - k + 1;
+        const int which = (int)((code >> (30 - 3 * top)) & 7u);
+        const int oct_parent = a.offsets[rp];
+        put_child(t, oct_parent, which, (((uint32_t)i << 4) | (uint32_t)(k - 1)) + 1u, z.n_oct,
+                  status);
+        if ((unsigned)oct_parent < (unsigned)z.n_oct) atomicOr(&t.mask[oct_parent], 1u << which);
+        const int slot = base + k - 1;
+        if ((unsigned)slot < (unsigned)z.n_oct) atomicMax(&t.owner[slot], (uint32_t)i);
+        else raise_status(status, kStatusCapacity);
+      }
+    }
+    if (mode & kOctLink) {
+      // include/shared/oct.h:92-134, walk bounded at radix node 0.
+      const bool l = a.hll[i], r = a.hlr[i];
+      if (l || r) {
+        int rn = i, steps = 0;
+        while (a.counts[rn] == 0 && rn != 0) {
+          const int up = a.parent[rn];
+          if ((unsigned)up >= (unsigned)z.n_brt || ++steps > 64) {
+            raise_status(status, kStatusWalkLimit);
+            break;
+          }
+          rn = up;
+        }
+        const int dst = a.offsets[rn];
+        const uint32_t sh = (uint32_t)(30 - 3 * (L + 1)) & 31u;
+        int lc = a.left_child[i];
+        if ((unsigned)lc >= (unsigned)z.n_brt) {  // leaf index lc + 1 <= n_brt must hold
+          raise_status(status, kStatusWalkLimit);
+          continue;
+        }
+        if (l)
+          put_child(t, dst, (int)((a.codes[lc] >> sh) & 7u), kLinkTag | ((uint32_t)i << 1),
+                    z.n_oct, status);
+        if (r)
+          put_child(t, dst, (int)((a.codes[lc + 1] >> sh) & 7u),
+                    kLinkTag | ((uint32_t)i << 1) | 1u, z.n_oct, status);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
+  const Sizes z = read_sizes(a);
+  if (!z.fits || z.n_brt < 1) return;
+  const int root_level = a.prefix_n[0] / 3;
+  const bool fresh = mode & kOctFresh;
+  const int stride = gridDim.x * blockDim.x;
+  const uint4* c4 = reinterpret_cast<const uint4*>(t.child);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < z.n_oct; p += stride) {
+    const uint4 ta = c4[2 * p], tb = c4[2 * p + 1];
+    const uint32_t tags[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+    oct_node* nd = a.nodes + p;
+    int ch[8];
+    uint32_t link_bits = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t g = tags[c];
+      if (g == 0) {
+        ch[c] = fresh ? 0 : nd->children[c];
+      } else if (g & kLinkTag) {
+        const int i = (int)((g & ~kLinkTag) >> 1);
+        ch[c] = a.left_child[i] + (int)(g & 1u);
+        link_bits |= 1u << c;
+      } else {
+        const uint32_t q = g - 1u;
+        ch[c] = a.offsets[q >> 4] + (int)(q & 15u);
+      }
+    }
+    const uint32_t m = t.mask[p];
+    const uint32_t own = t.owner[p];
+    float4 corner;
+    float cell;
+    if (own != 0) {
+      const int i = (int)own;
+      const int j = p - a.offsets[i];
+      const int level = a.prefix_n[i] / 3 - j;
+      const int sh = 30 - 3 * level;
+      corner = decode_corner((a.codes[i] >> sh) << sh, a.min_coord, a.range);
+      cell = __fdiv_rn(a.range, (float)(1 << (level - root_level)));
+    } else if (fresh && p == 0) {
+      const int sh = 30 - 3 * root_level;
+      corner = decode_corner((a.codes[0] >> sh) << sh, a.min_coord, a.range);
+      cell = a.range;
+    } else if (fresh) {
+      corner = make_float4(0.f, 0.f, 0.f, 0.f);
+      cell = 0.f;
+    } else {
+      corner = make_float4(nd->corner.x, nd->corner.y, nd->corner.z, nd->corner.w);
+      cell = nd->cell_size;
+    }
+    int node_mask, leaf_mask;
+    if (fresh) {
+      node_mask = (int)m;
+      leaf_mask = 0;
+    } else {
+      node_mask = nd->child_node_mask | (int)m;
+      leaf_mask = nd->child_leaf_mask & ~(int)link_bits;
+    }
+    // 60-byte node as 15 consecutive 32-bit stores.
+    int* w = reinterpret_cast<int*>(nd);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) w[c] = ch[c];
+    w[8] = __float_as_int(corner.x);
+    w[9] = __float_as_int(corner.y);
+    w[10] = __float_as_int(corner.z);
+    w[11] = __float_as_int(corner.w);
+    w[12] = __float_as_int(cell);
+    w[13] = node_mask;
+    w[14] = leaf_mask;
+  }
+}
+
+cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t* status,
+                          cudaStream_t s, Recorder* rec) {
+  const int sms = device_sm_count();
+  const int zgrid = sms * 8;
+  oct_zero_kernel<<<zgrid, 256, 0, s>>>(a, t, status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mark(rec, s);
+  int nb = a.d_unique ? a.n_brt_host : a.n_brt_host;
+  int egrid = (nb + 255) / 256;
+  if (egrid < 1) egrid = 1;
+  oct_emit_kernel<<<egrid, 256, 0, s>>>(mode, a, t, status);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mark(rec, s);
+  int fgrid = (a.cap + 255) / 256;
+  if (fgrid < 1) fgrid = 1;
+  oct_finalize_kernel<<<fgrid, 256, 0, s>>>(mode, a, t);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) mark(rec, s);
+  return e;
+}
+
+__global__ void publish_counts_kernel(const int* d_unique, const int* d_max_slot,
+                                      const uint32_t* status, int* out) {
+  const int u = *d_unique;
+  const int b = max(u - 1, 0);
+  out[0] = u;
+  out[1] = b;
+  out[2] = b >= 1 ? *d_max_slot + 1 : 0;
+  out[3] = status ? (int)*status : 0;
+}
+
+cudaError_t launch_publish_counts(const int* d_unique, const int* d_max_slot,
+                                  const uint32_t* status, int* out, cudaStream_t s) {
+  publish_counts_kernel<<<1, 1, 0, s>>>(d_unique, d_max_slot, status, out);
+  return cudaGetLastError();
+}
+
+}  // namespace octgb

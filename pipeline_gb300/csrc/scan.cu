@@ -1,0 +1,338 @@
+// Stage 3 (unique) and stages 5-6 (edge count + inclusive prefix sum).
+//
+// Both are single-pass tile scans with decoupled look-back: a tile takes the
+// next id from an atomic counter, reduces its items, publishes its aggregate,
+// waits (bounded) for the inclusive prefix of the tiles before it and writes.
+//
+// Unique replaces k_CountUnique (reference include/kernels/03_unique.hpp:4,
+// kernels/03_unique.cpp:2-16; the reference GPU form is one thread,
+// kernels/cuda/03_unique.cu:5-24). It may run in place: every output position
+// is at or before its input position, and a tile writes only after the tiles
+// before it published their aggregates, which they do after loading.
+//
+// Edge count + prefix sum replace k_EdgeCount
+// (include/kernels/05_edge_count.hpp:5-8) and k_PartialSum
+// (include/kernels/06_partial_sum.hpp:6-9; the reference GPU driver does this
+// scan on the host, apps/gpu_demo/main.cu:308-310). Fused, one read of
+// prefix_n/parent produces both arrays and the octree node count.
+#include "kernels.cuh"
+
+namespace octgb {
+
+constexpr unsigned long long kLbAgg = 1ull << 62;
+constexpr unsigned long long kLbInc = 2ull << 62;
+constexpr unsigned long long kLbFlags = 3ull << 62;
+
+// One thread per tile: publish the tile aggregate, return the exclusive prefix.
+__device__ uint32_t lookback_u32(unsigned long long* lb, int tile, uint32_t agg,
+                                 uint32_t* status) {
+  if (tile == 0) {
+    st_release_u64(lb, kLbInc | agg);
+    return 0;
+  }
+  st_release_u64(lb + tile, kLbAgg | agg);
+  uint32_t ex = 0;
+  int pred = tile - 1;
+  uint32_t spins = 0;
+  while (pred >= 0) {
+    const unsigned long long w = ld_acquire_u64(lb + pred);
+    const unsigned long long f = w & kLbFlags;
+    if (f == 0) {
+      if (++spins > kSpinLimit) {
+        raise_status(status, kStatusSpinTimeout);
+        break;
+      }
+      backoff(spins);
+      continue;
+    }
+    ex += (uint32_t)w;
+    if (f == kLbInc) break;
+    --pred;
+  }
+  st_release_u64(lb + tile, kLbInc | (uint32_t)(ex + agg));
+  return ex;
+}
+
+// --------------------------------------------------------------------------
+// Unique.
+// --------------------------------------------------------------------------
+constexpr int kUqThreads = 256;
+constexpr int kUqItems = 16;
+constexpr int kUqTile = kUqThreads * kUqItems;
+
+__device__ __forceinline__ int pad_idx(int j) { return j + (j >> 5); }
+
+__global__ void __launch_bounds__(kUqThreads)
+    unique_kernel(const uint32_t* src, uint32_t* dst, int n, int* __restrict__ d_count,
+                  unsigned long long* __restrict__ lb, uint32_t* __restrict__ counter, int tiles,
+                  uint32_t* __restrict__ status) {
+  __shared__ uint32_t s_keys[kUqTile + kUqTile / 32];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_misc[4];
+  const int tid = threadIdx.x;
+  if (tid == 0) s_misc[0] = atomicAdd(counter, 1u);
+  __syncthreads();
+  const int tile = (int)s_misc[0];
+  const int start = tile * kUqTile;
+  const int valid = min(kUqTile, n - start);
+  // Coalesced load into padded shared memory (plus the key before the tile).
+#pragma unroll 4
+  for (int j = tid; j < kUqTile; j += kUqThreads) {
+    const int idx = start + j;
+    s_keys[pad_idx(j)] = idx < n ? src[idx] : 0u;
+  }
+  uint32_t before = 0;
+  if (tid == 0 && start > 0) before = src[start - 1];
+  if (tid == 0) s_misc[1] = before;
+  __syncthreads();
+  // Blocked flags: item j = tid * ITEMS + k is a run head if it differs from j - 1.
+  uint32_t key[kUqItems];
+  uint32_t flags = 0;
+  int cnt = 0;
+  const int j0 = tid * kUqItems;
+  uint32_t prev = j0 == 0 ? s_misc[1] : s_keys[pad_idx(j0 - 1)];
+#pragma unroll
+  for (int k = 0; k < kUqItems; ++k) {
+    key[k] = s_keys[pad_idx(j0 + k)];
+    const int j = j0 + k;
+    const bool head = j < valid && ((start + j == 0) || key[k] != prev);
+    flags |= (uint32_t)head << k;
+    cnt += head;
+    prev = key[k];
+  }
+  uint32_t total;
+  const uint32_t off = block_exclusive_sum<kUqThreads>((uint32_t)cnt, s_warp, &s_misc[2]);
+  total = s_misc[2];
+  if (tid == 0) s_misc[3] = lookback_u32(lb, tile, total, status);
+  // Stage the tile's run heads contiguously (s_keys is free after the scan's barriers).
+  uint32_t o = off;
+#pragma unroll
+  for (int k = 0; k < kUqItems; ++k)
+    if (flags >> k & 1u) s_keys[pad_idx(o++)] = key[k];
+  __syncthreads();
+  const uint32_t ex = s_misc[3];
+  for (int j = tid; j < (int)total; j += kUqThreads) dst[ex + j] = s_keys[pad_idx(j)];
+  if (tid == 0 && tile == tiles - 1) *d_count = (int)(ex + total);
+}
+
+ScanPlan unique_plan(int n) {
+  ScanPlan p{};
+  p.n = n;
+  p.tile = kUqTile;
+  p.tiles = n > 0 ? (n + kUqTile - 1) / kUqTile : 0;
+  p.counter_off = 0;
+  p.lookback_off = 256;
+  p.bytes = align_up(p.lookback_off + sizeof(unsigned long long) * (size_t)(p.tiles + 1), 256);
+  return p;
+}
+
+cudaError_t launch_unique(const uint32_t* src, uint32_t* dst, int n, int* d_count,
+                          const ScanPlan* plan, void* ctrl, uint32_t* status, cudaStream_t s) {
+  if (n <= 0) return cudaMemsetAsync(d_count, 0, sizeof(int), s);
+  char* c = static_cast<char*>(ctrl);
+  unique_kernel<<<plan->tiles, kUqThreads, 0, s>>>(
+      src, dst, n, d_count, reinterpret_cast<unsigned long long*>(c + plan->lookback_off),
+      reinterpret_cast<uint32_t*>(c + plan->counter_off), plan->tiles, status);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------------------------
+// Edge count + inclusive prefix sum.
+// --------------------------------------------------------------------------
+constexpr int kEsThreads = 256;
+constexpr int kEsItems = 16;
+constexpr int kEsTile = kEsThreads * kEsItems;
+
+__global__ void __launch_bounds__(kEsThreads)
+    edge_scan_kernel(int mode, int n_host, const int* __restrict__ d_unique,
+                     const uint8_t* __restrict__ prefix_n, const int* __restrict__ parent,
+                     int* ec_out, int* __restrict__ ps_out, int* __restrict__ d_max_slot,
+                     unsigned long long* __restrict__ lb, uint32_t* __restrict__ counter,
+                     uint32_t* __restrict__ status) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_misc[4];
+  __shared__ int s_max[kEsThreads / 32];
+  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
+  const int tid = threadIdx.x;
+  // Edge count alone has no cross-tile dependency: the block index is the tile.
+  if (tid == 0) s_misc[0] = mode == kEdgeOnly ? blockIdx.x : atomicAdd(counter, 1u);
+  __syncthreads();
+  const int tile = (int)s_misc[0];
+  const int start = tile * kEsTile;
+  if (start >= n) return;  // tiles past the end: nobody waits on them
+  const int tiles = (n + kEsTile - 1) / kEsTile;
+  const int j0 = start + tid * kEsItems;
+
+  int v[kEsItems];
+  if (mode & kEdgeOnly) {
+#pragma unroll
+    for (int k = 0; k < kEsItems; ++k) {
+      const int i = j0 + k;
+      int e = 0;
+      if (i > 0 && i < n) {
+        int p = parent[i];
+        if ((unsigned)p >= (unsigned)n) {  // malformed input: never read out of bounds
+          raise_status(status, kStatusWalkLimit);
+          p = 0;
+        }
+        e = (int)(prefix_n[i] / 3) - (int)(prefix_n[p] / 3);
+      }
+      v[k] = e;
+    }
+    if (!(mode & kScanOnly)) {
+#pragma unroll
+      for (int k = 0; k < kEsItems; ++k)
+        if (j0 + k < n) ec_out[j0 + k] = v[k];
+      return;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kEsItems; ++k) v[k] = j0 + k < n ? ec_out[j0 + k] : 0;
+  }
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kEsItems; ++k) sum += (uint32_t)v[k];
+  const uint32_t off = block_exclusive_sum<kEsThreads>(sum, s_warp, &s_misc[2]);
+  if (tid == 0) s_misc[3] = lookback_u32(lb, tile, s_misc[2], status);
+  __syncthreads();
+  uint32_t run = s_misc[3] + off;
+  int mx = 0;
+#pragma unroll
+  for (int k = 0; k < kEsItems; ++k) {
+    const int i = j0 + k;
+    run += (uint32_t)v[k];
+    if (i < n) {
+      if (mode == kEdgeAndScan) ec_out[i] = v[k];
+      ps_out[i] = (int)run;
+      const int last = v[k] > 0 ? (int)run + v[k] - 1 : (int)run;
+      if (i > 0 && v[k] > 0 && last > mx) mx = last;
+      if (i == n - 1 && (int)run > mx) mx = (int)run;
+    }
+  }
+  if (d_max_slot) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) s_max[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+      int m = 0;
+      for (int w = 0; w < kEsThreads / 32; ++w) m = max(m, s_max[w]);
+      atomicMax(d_max_slot, m);
+    }
+  }
+  (void)tiles;
+}
+
+ScanPlan edge_scan_plan(int n) {
+  ScanPlan p{};
+  p.n = n;
+  p.tile = kEsTile;
+  p.tiles = n > 0 ? (n + kEsTile - 1) / kEsTile : 0;
+  p.counter_off = 0;
+  p.lookback_off = 256;
+  p.bytes = align_up(p.lookback_off + sizeof(unsigned long long) * (size_t)(p.tiles + 1), 256);
+  return p;
+}
+
+cudaError_t launch_edge_scan(int mode, int n_host, const int* d_unique, const uint8_t* prefix_n,
+                             const int* parent, int* ec, int* ps, int* d_max_slot,
+                             const ScanPlan* plan, void* ctrl, uint32_t* status, cudaStream_t s) {
+  if (plan->tiles <= 0) return cudaSuccess;
+  char* c = static_cast<char*>(ctrl);
+  unsigned long long* lb =
+      c ? reinterpret_cast<unsigned long long*>(c + plan->lookback_off) : nullptr;
+  uint32_t* counter = c ? reinterpret_cast<uint32_t*>(c + plan->counter_off) : nullptr;
+  if (mode != kEdgeOnly && !c) return cudaErrorInvalidValue;
+  edge_scan_kernel<<<plan->tiles, kEsThreads, 0, s>>>(mode, n_host, d_unique, prefix_n, parent,
+                                                      ec, ps, d_max_slot, lb, counter, status);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------------------------
+// Karras radix tree (stage 4), one thread per node.
+// Replaces k_BuildRadixTree (include/kernels/04_radix_tree.hpp:5-11,
+// kernels/04_radix_tree.cpp:39-121). The search steps are the reference's,
+// step for step, since its root convention (d = 1, l = n - 1) and cut-offs
+// show in the output.
+//
+// Parent writes: only radix nodes 0 and n-1 can claim the same children, and
+// only when the root, which spans keys [0, n-1], has a longer common prefix
+// than keys [0, n] ("short root"); then node n-1 spans the same range, makes
+// the same split and, being later, wins. Node 0 therefore skips its parent
+// writes in that case. Entries nobody writes are parent[0] and, when the
+// root is short or its right child is the leaf n-1, parent[n-1]; node 0
+// zeroes exactly those, so no pre-clear of parent[] is needed.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void radix_node(int i, int n, const uint32_t* __restrict__ codes,
+                                           uint8_t* __restrict__ prefix_n,
+                                           uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
+                                           int* __restrict__ left_child,
+                                           int* __restrict__ parent) {
+  const uint32_t ci = codes[i];
+  int d, l = 0;
+  if (i == 0) {
+    d = 1;
+    l = n - 1;
+  } else {
+    const int diff = delta_u8(ci, codes[i + 1]) - delta_u8(ci, codes[i - 1]);
+    d = (diff > 0) - (diff < 0);
+    const int dmin = delta_u8(ci, codes[i - d]);
+    int lmax = 2;
+    while (true) {
+      const long long e = (long long)i + (long long)lmax * d;
+      if (e < 0 || e > n || delta_u8(ci, codes[e]) <= dmin) break;
+      lmax *= 2;
+    }
+    const int lcut = (d == -1) ? i : n - i;
+    for (unsigned div = 2, t = (unsigned)lmax / 2; t >= 1; div *= 2, t = (unsigned)lmax / div)
+      if (l + (int)t <= lcut && delta_u8(ci, codes[i + (l + (int)t) * d]) > dmin) l += (int)t;
+  }
+  const int j = i + l * d;
+  const int dnode = delta_u8(ci, codes[j]);
+  prefix_n[i] = (uint8_t)dnode;
+  int s = 0;
+  if (l > 0) {
+    const unsigned maxdiv = 1u << log2_ceil_u32((uint32_t)l);
+    const int scut = (d == -1) ? i - 1 : n - i - 1;
+    for (unsigned div = 2, t = ((unsigned)l + 1) / 2; div <= maxdiv;
+         div <<= 1, t = ((unsigned)l + div - 1) / div)
+      if (s + (int)t <= scut && delta_u8(ci, codes[i + (s + (int)t) * d]) > dnode) s += (int)t;
+  }
+  const int gamma = i + s * d + min(d, 0);
+  left_child[i] = gamma;
+  const bool leaf_l = min(i, j) == gamma;
+  const bool leaf_r = max(i, j) == gamma + 1;
+  hll[i] = leaf_l;
+  hlr[i] = leaf_r;
+  if (i == 0) {
+    parent[0] = 0;
+    const bool short_root = n >= 2 && delta_u8(ci, codes[n - 1]) > delta_u8(ci, codes[n]);
+    if (n >= 2 && (short_root || leaf_r)) parent[n - 1] = 0;
+    if (short_root) return;
+  }
+  if (!leaf_l && gamma < n) parent[gamma] = i;
+  if (!leaf_r && gamma + 1 < n) parent[gamma + 1] = i;
+}
+
+__global__ void __launch_bounds__(256)
+    radix_tree_kernel(int n_host, const int* __restrict__ d_unique,
+                      const uint32_t* __restrict__ codes, uint8_t* __restrict__ prefix_n,
+                      uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
+                      int* __restrict__ left_child, int* __restrict__ parent) {
+  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    radix_node(i, n, codes, prefix_n, hll, hlr, left_child, parent);
+}
+
+cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* codes,
+                              uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
+                              int* parent, cudaStream_t s) {
+  if (n_host <= 0) return cudaSuccess;
+  const int grid = (n_host + 255) / 256;
+  radix_tree_kernel<<<grid, 256, 0, s>>>(n_host, d_unique, codes, prefix_n, hll, hlr,
+                                         left_child, parent);
+  return cudaGetLastError();
+}
+
+}  // namespace octgb
