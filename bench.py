@@ -260,6 +260,10 @@ def run_ours(args, rank, world, local_rank):
     names = [lib.oct_build_step_name(i).decode() for i in range(nsteps)]
     reps = max(3, min(args.steps, 10))
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(nsteps)] for _ in range(reps)]
+    for row in evs:  # torch creates the CUDA event on its first record
+        for e in row:
+            e.record(stream)
+    torch.cuda.synchronize(dev)
     for r in range(reps):
         flush.fill_(r & 0xFF)
         handles = (C.c_void_p * nsteps)(*[e.cuda_event for e in evs[r]])
@@ -341,6 +345,23 @@ def run_ours(args, rank, world, local_rank):
     return 0
 
 
+def profile_only(args):
+    """--warmup builds then exactly one more build of the workload: a short,
+    fixed launch sequence for ncu (12 kernel launches per build)."""
+    import torch
+
+    from pipeline_gb300.pipeline import OctreeBuilder
+
+    pts = torch.from_numpy(make_points(N_POINTS)).cuda()
+    b = OctreeBuilder(N_POINTS)
+    for _ in range(max(args.warmup, 0) + 1):
+        b.build(pts, MIN_COORD, RANGE)
+    torch.cuda.synchronize()
+    c = b.counts()
+    print(f"profile build: U={c.n_unique} M={c.n_oct} status={c.status}")
+    return 0 if c.status == 0 else 1
+
+
 def read_traffic(kernel_step: str, n: int):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (profiles/dram_traffic.txt: '<step name>|<bytes per launch>|<n>'),
@@ -363,7 +384,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="warm-up builds plus one build, no timing or output (for ncu captures)")
     args = ap.parse_args()
+    if args.profile_only:
+        return profile_only(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -406,7 +406,12 @@ int oct_build_octree_timed(const oct_vec4* points, int n, float min_coord, float
   Recorder r;
   r.events = reinterpret_cast<cudaEvent_t*>(const_cast<void**>(events));
   r.n = n_events;
-  return build_impl(points, n, min_coord, range, out, workspace, workspace_bytes, stream, &r);
+  const int rc = build_impl(points, n, min_coord, range, out, workspace, workspace_bytes, stream, &r);
+  if (rc == OCT_OK && r.err != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(r.err, "oct_build_octree_timed: event record");
+  }
+  return rc;
 }
 
 

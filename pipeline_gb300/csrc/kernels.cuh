@@ -19,8 +19,9 @@ struct Recorder {
   cudaEvent_t* events = nullptr;
   int n = 0;
   int k = 0;
+  cudaError_t err = cudaSuccess;
   void mark(cudaStream_t s) {
-    if (k < n) cudaEventRecord(events[k], s);
+    if (k < n && err == cudaSuccess) err = cudaEventRecord(events[k], s);
     ++k;
   }
 };
