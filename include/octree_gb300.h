@@ -81,7 +81,8 @@ typedef enum oct_status {
   OCT_ERR_WORKSPACE = 2,   /* workspace smaller than *_workspace_bytes() */
   OCT_ERR_CUDA = 3,        /* a CUDA runtime call or launch failed */
   OCT_ERR_DEVICE = 4,      /* the device status word is non-zero (sync calls) */
-  OCT_ERR_CAPACITY = 5     /* octree node buffer too small (sync calls) */
+  OCT_ERR_CAPACITY = 5,    /* octree node buffer too small (sync calls) */
+  OCT_ERR_TOO_LARGE = 6    /* size above a fixed limit (oct_sort_keys_noalloc) */
 } oct_status;
 
 /* Device status word bits. */
@@ -126,6 +127,20 @@ OCT_API int oct_morton_encode(const oct_vec4* points, uint32_t* keys, int64_t n,
 OCT_API size_t oct_sort_workspace_bytes(int n, int key_bits);
 OCT_API int oct_sort_keys(uint32_t* keys, uint32_t* keys_alt, int n, int key_bits, void* workspace,
                   size_t workspace_bytes, uint32_t* d_status, oct_stream_t stream);
+
+/* Allocation-free variant of oct_sort_keys, for callers that cannot call
+ * cudaMalloc (device memory owned by another allocator or a fixed pool; frame
+ * loops where an allocation would stall the device). No counterpart in the
+ * reference. Same keys / keys_alt / key_bits semantics; the scratch lives in
+ * a fixed 6.5 MiB __device__ array inside the library, which every GPU that
+ * loads the library holds until exit. n above OCT_NOALLOC_SORT_MAX_KEYS
+ * returns OCT_ERR_TOO_LARGE. The first call on a device sets up the array's
+ * address; make it before any stream capture. Calls share the array: calls
+ * that overlap on the GPU race. */
+#define OCT_NOALLOC_SORT_MAX_KEYS (1 << 22)
+#define OCT_NOALLOC_SORT_SCRATCH_BYTES (6815744u)
+OCT_API int oct_sort_keys_noalloc(uint32_t* keys, uint32_t* keys_alt, int n, int key_bits,
+                                  uint32_t* d_status, oct_stream_t stream);
 
 /* ----------------------------------------------------------------------- */
 /* Stage 3: unique. Replaces k_CountUnique (include/kernels/03_unique.hpp:4,*/

@@ -19,6 +19,7 @@ OCT_ERR_WORKSPACE = 2
 OCT_ERR_CUDA = 3
 OCT_ERR_DEVICE = 4
 OCT_ERR_CAPACITY = 5
+OCT_ERR_TOO_LARGE = 6
 
 OCT_STATUS_SPIN_TIMEOUT = 1
 OCT_STATUS_WALK_LIMIT = 2
@@ -78,6 +79,7 @@ SIGNATURES = {
     "oct_morton_encode": (I, [P, P, C.c_int64, F, F, P, P]),
     "oct_sort_workspace_bytes": (Z, [I, I]),
     "oct_sort_keys": (I, [P, P, I, I, P, Z, P, P]),
+    "oct_sort_keys_noalloc": (I, [P, P, I, I, P, P]),
     "oct_unique_workspace_bytes": (Z, [I]),
     "oct_unique": (I, [P, I, P, P, Z, P, P]),
     "oct_build_radix_tree": (I, [I, P, P, P, P, P, P, P]),

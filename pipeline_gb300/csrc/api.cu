@@ -94,6 +94,10 @@ __global__ void root_init_kernel(oct_node* nodes, const uint32_t* codes, const u
 
 }  // namespace
 
+void octgb::set_last_error(const char* msg) {
+  snprintf(g_last_error, sizeof(g_last_error), "%s", msg);
+}
+
 static_assert(sizeof(oct_node) == 60, "oct_node must match OctNode (60 bytes)");
 static_assert(offsetof(oct_node, corner) == 32, "OctNode::corner at byte 32");
 static_assert(offsetof(oct_node, cell_size) == 48, "OctNode::cell_size at byte 48");

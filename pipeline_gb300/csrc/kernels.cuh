@@ -31,6 +31,9 @@ static inline void mark(Recorder* r, cudaStream_t s) {
 
 int device_sm_count();
 
+// Sets the text oct_last_error() returns on this thread.
+void set_last_error(const char* msg);
+
 // ---- sort ----------------------------------------------------------------
 struct SortPlan {
   int n;
