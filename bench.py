@@ -352,8 +352,9 @@ def profile_only(args):
 
     from pipeline_gb300.pipeline import OctreeBuilder
 
-    pts = torch.from_numpy(make_points(N_POINTS)).cuda()
-    b = OctreeBuilder(N_POINTS)
+    n = int(args.points)
+    pts = torch.from_numpy(make_points(n)).cuda()
+    b = OctreeBuilder(n)
     for _ in range(max(args.warmup, 0) + 1):
         b.build(pts, MIN_COORD, RANGE)
     torch.cuda.synchronize()
@@ -386,6 +387,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up builds plus one build, no timing or output (for ncu captures)")
+    ap.add_argument("--points", type=int, default=N_POINTS,
+                    help="cloud size for --profile-only (smaller cases for multi-pass ncu captures)")
     args = ap.parse_args()
     if args.profile_only:
         return profile_only(args)

@@ -165,74 +165,84 @@ __global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctT
   }
 }
 
-__global__ void __launch_bounds__(256) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
+// One thread per slot computes the node; the block stages its 256 nodes
+// (15 KB) in shared memory and writes them as consecutive 32-bit words, so
+// every warp store is one contiguous 128-byte line.
+constexpr int kFinThreads = 256;
+constexpr int kNodeWords = 15;
+
+__global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
+  __shared__ int s_nodes[kFinThreads * kNodeWords];
   const Sizes z = read_sizes(a);
   if (!z.fits || z.n_brt < 1) return;
   const int root_level = a.prefix_n[0] / 3;
   const bool fresh = mode & kOctFresh;
-  const int stride = gridDim.x * blockDim.x;
   const uint4* c4 = reinterpret_cast<const uint4*>(t.child);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < z.n_oct; p += stride) {
-    const uint4 ta = c4[2 * p], tb = c4[2 * p + 1];
-    const uint32_t tags[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
-    oct_node* nd = a.nodes + p;
-    int ch[8];
-    uint32_t link_bits = 0;
+  int* out_words = reinterpret_cast<int*>(a.nodes);
+  for (int blk = blockIdx.x * kFinThreads; blk < z.n_oct; blk += gridDim.x * kFinThreads) {
+    const int p = blk + threadIdx.x;
+    const int count = min(kFinThreads, z.n_oct - blk);
+    if (p < z.n_oct) {
+      const uint4 ta = c4[2 * p], tb = c4[2 * p + 1];
+      const uint32_t tags[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+      const oct_node* nd = a.nodes + p;
+      int* w = s_nodes + threadIdx.x * kNodeWords;
+      uint32_t link_bits = 0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      const uint32_t g = tags[c];
-      if (g == 0) {
-        ch[c] = fresh ? 0 : nd->children[c];
-      } else if (g & kLinkTag) {
-        const int i = (int)((g & ~kLinkTag) >> 1);
-        ch[c] = a.left_child[i] + (int)(g & 1u);
-        link_bits |= 1u << c;
+      for (int c = 0; c < 8; ++c) {
+        const uint32_t g = tags[c];
+        int v;
+        if (g == 0) {
+          v = fresh ? 0 : nd->children[c];
+        } else if (g & kLinkTag) {
+          const int i = (int)((g & ~kLinkTag) >> 1);
+          v = a.left_child[i] + (int)(g & 1u);
+          link_bits |= 1u << c;
+        } else {
+          const uint32_t q = g - 1u;
+          v = a.offsets[q >> 4] + (int)(q & 15u);
+        }
+        w[c] = v;
+      }
+      const uint32_t m = t.mask[p];
+      const uint32_t own = t.owner[p];
+      float4 corner;
+      float cell;
+      if (own != 0) {
+        const int i = (int)own;
+        const int j = p - a.offsets[i];
+        const int level = a.prefix_n[i] / 3 - j;
+        const int sh = 30 - 3 * level;
+        corner = decode_corner((a.codes[i] >> sh) << sh, a.min_coord, a.range);
+        cell = __fdiv_rn(a.range, (float)(1 << (level - root_level)));
+      } else if (fresh && p == 0) {
+        const int sh = 30 - 3 * root_level;
+        corner = decode_corner((a.codes[0] >> sh) << sh, a.min_coord, a.range);
+        cell = a.range;
+      } else if (fresh) {
+        corner = make_float4(0.f, 0.f, 0.f, 0.f);
+        cell = 0.f;
       } else {
-        const uint32_t q = g - 1u;
-        ch[c] = a.offsets[q >> 4] + (int)(q & 15u);
+        corner = make_float4(nd->corner.x, nd->corner.y, nd->corner.z, nd->corner.w);
+        cell = nd->cell_size;
+      }
+      w[8] = __float_as_int(corner.x);
+      w[9] = __float_as_int(corner.y);
+      w[10] = __float_as_int(corner.z);
+      w[11] = __float_as_int(corner.w);
+      w[12] = __float_as_int(cell);
+      if (fresh) {
+        w[13] = (int)m;
+        w[14] = 0;
+      } else {
+        w[13] = nd->child_node_mask | (int)m;
+        w[14] = nd->child_leaf_mask & ~(int)link_bits;
       }
     }
-    const uint32_t m = t.mask[p];
-    const uint32_t own = t.owner[p];
-    float4 corner;
-    float cell;
-    if (own != 0) {
-      const int i = (int)own;
-      const int j = p - a.offsets[i];
-      const int level = a.prefix_n[i] / 3 - j;
-      const int sh = 30 - 3 * level;
-      corner = decode_corner((a.codes[i] >> sh) << sh, a.min_coord, a.range);
-      cell = __fdiv_rn(a.range, (float)(1 << (level - root_level)));
-    } else if (fresh && p == 0) {
-      const int sh = 30 - 3 * root_level;
-      corner = decode_corner((a.codes[0] >> sh) << sh, a.min_coord, a.range);
-      cell = a.range;
-    } else if (fresh) {
-      corner = make_float4(0.f, 0.f, 0.f, 0.f);
-      cell = 0.f;
-    } else {
-      corner = make_float4(nd->corner.x, nd->corner.y, nd->corner.z, nd->corner.w);
-      cell = nd->cell_size;
-    }
-    int node_mask, leaf_mask;
-    if (fresh) {
-      node_mask = (int)m;
-      leaf_mask = 0;
-    } else {
-      node_mask = nd->child_node_mask | (int)m;
-      leaf_mask = nd->child_leaf_mask & ~(int)link_bits;
-    }
-    // 60-byte node as 15 consecutive 32-bit stores.
-    int* w = reinterpret_cast<int*>(nd);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) w[c] = ch[c];
-    w[8] = __float_as_int(corner.x);
-    w[9] = __float_as_int(corner.y);
-    w[10] = __float_as_int(corner.z);
-    w[11] = __float_as_int(corner.w);
-    w[12] = __float_as_int(cell);
-    w[13] = node_mask;
-    w[14] = leaf_mask;
+    __syncthreads();
+    int* dst = out_words + (size_t)blk * kNodeWords;
+    for (int k = threadIdx.x; k < count * kNodeWords; k += kFinThreads) dst[k] = s_nodes[k];
+    __syncthreads();
   }
 }
 
@@ -251,9 +261,9 @@ cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(rec, s);
-  int fgrid = (a.cap + 255) / 256;
+  int fgrid = (a.cap + kFinThreads - 1) / kFinThreads;
   if (fgrid < 1) fgrid = 1;
-  oct_finalize_kernel<<<fgrid, 256, 0, s>>>(mode, a, t);
+  oct_finalize_kernel<<<fgrid, kFinThreads, 0, s>>>(mode, a, t);
   e = cudaGetLastError();
   if (e == cudaSuccess) mark(rec, s);
   return e;

@@ -23,33 +23,44 @@ constexpr unsigned long long kLbAgg = 1ull << 62;
 constexpr unsigned long long kLbInc = 2ull << 62;
 constexpr unsigned long long kLbFlags = 3ull << 62;
 
-// One thread per tile: publish the tile aggregate, return the exclusive prefix.
-__device__ uint32_t lookback_u32(unsigned long long* lb, int tile, uint32_t agg,
-                                 uint32_t* status) {
+// One full warp per tile: lane l probes predecessor (pred - l) with a relaxed
+// load (flag and value share a 64-bit word), so one round trip covers 32
+// predecessors. Returns the exclusive prefix in every lane; lane 0 publishes.
+__device__ uint32_t warp_lookback_u32(unsigned long long* lb, int tile, uint32_t agg,
+                                      uint32_t* status) {
+  const int lane = threadIdx.x & 31;
   if (tile == 0) {
-    st_release_u64(lb, kLbInc | agg);
+    if (lane == 0) st_release_u64(lb, kLbInc | agg);
     return 0;
   }
-  st_release_u64(lb + tile, kLbAgg | agg);
+  if (lane == 0) st_release_u64(lb + tile, kLbAgg | agg);
   uint32_t ex = 0;
   int pred = tile - 1;
   uint32_t spins = 0;
-  while (pred >= 0) {
-    const unsigned long long w = ld_acquire_u64(lb + pred);
+  while (true) {
+    const int p = pred - lane;
+    const unsigned long long w = p >= 0 ? ld_relaxed_u64(lb + p) : kLbInc;
     const unsigned long long f = w & kLbFlags;
-    if (f == 0) {
+    const uint32_t inc_m = __ballot_sync(0xffffffffu, f == kLbInc);
+    const uint32_t nr_m = __ballot_sync(0xffffffffu, f == 0);
+    const int first_inc = inc_m ? __ffs(inc_m) - 1 : 32;
+    const int first_nr = nr_m ? __ffs(nr_m) - 1 : 32;
+    if (first_nr < first_inc) {  // take the ready words before it, wait on it
+      ex += __reduce_add_sync(0xffffffffu, lane < first_nr ? (uint32_t)w : 0u);
+      pred -= first_nr;
       if (++spins > kSpinLimit) {
-        raise_status(status, kStatusSpinTimeout);
+        if (lane == 0) raise_status(status, kStatusSpinTimeout);
         break;
       }
       backoff(spins);
       continue;
     }
-    ex += (uint32_t)w;
-    if (f == kLbInc) break;
-    --pred;
+    const int take = first_inc < 32 ? first_inc + 1 : 32;
+    ex += __reduce_add_sync(0xffffffffu, lane < take ? (uint32_t)w : 0u);
+    if (first_inc < 32) break;
+    pred -= 32;
   }
-  st_release_u64(lb + tile, kLbInc | (uint32_t)(ex + agg));
+  if (lane == 0) st_release_u64(lb + tile, kLbInc | (uint32_t)(ex + agg));
   return ex;
 }
 
@@ -103,7 +114,10 @@ __global__ void __launch_bounds__(kUqThreads)
   uint32_t total;
   const uint32_t off = block_exclusive_sum<kUqThreads>((uint32_t)cnt, s_warp, &s_misc[2]);
   total = s_misc[2];
-  if (tid == 0) s_misc[3] = lookback_u32(lb, tile, total, status);
+  if (tid < 32) {
+    const uint32_t e = warp_lookback_u32(lb, tile, total, status);
+    if (tid == 0) s_misc[3] = e;
+  }
   // Stage the tile's run heads contiguously (s_keys is free after the scan's barriers).
   uint32_t o = off;
 #pragma unroll
@@ -164,26 +178,70 @@ __global__ void __launch_bounds__(kEsThreads)
   const int j0 = start + tid * kEsItems;
 
   int v[kEsItems];
+  // A thread's 16 items are contiguous: 128-bit loads when in range and aligned.
+  const bool vec = j0 + kEsItems <= n &&
+                   ((reinterpret_cast<uintptr_t>(prefix_n) | reinterpret_cast<uintptr_t>(parent) |
+                     reinterpret_cast<uintptr_t>(ec_out) | reinterpret_cast<uintptr_t>(ps_out)) &
+                    15u) == 0;
   if (mode & kEdgeOnly) {
+    int par[kEsItems];
+    uint8_t pn[kEsItems];
+    if (vec) {
+      const uint4 pb = *reinterpret_cast<const uint4*>(prefix_n + j0);
+      const uint32_t pw[4] = {pb.x, pb.y, pb.z, pb.w};
+#pragma unroll
+      for (int k = 0; k < kEsItems; ++k) pn[k] = (uint8_t)(pw[k >> 2] >> (8 * (k & 3)));
+#pragma unroll
+      for (int q = 0; q < kEsItems / 4; ++q) {
+        const int4 t = *reinterpret_cast<const int4*>(parent + j0 + 4 * q);
+        par[4 * q] = t.x;
+        par[4 * q + 1] = t.y;
+        par[4 * q + 2] = t.z;
+        par[4 * q + 3] = t.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kEsItems; ++k) {
+        const int i = j0 + k;
+        pn[k] = i < n ? prefix_n[i] : 0;
+        par[k] = i < n ? parent[i] : 0;
+      }
+    }
 #pragma unroll
     for (int k = 0; k < kEsItems; ++k) {
       const int i = j0 + k;
       int e = 0;
       if (i > 0 && i < n) {
-        int p = parent[i];
+        int p = par[k];
         if ((unsigned)p >= (unsigned)n) {  // malformed input: never read out of bounds
           raise_status(status, kStatusWalkLimit);
           p = 0;
         }
-        e = (int)(prefix_n[i] / 3) - (int)(prefix_n[p] / 3);
+        e = (int)(pn[k] / 3) - (int)(prefix_n[p] / 3);
       }
       v[k] = e;
     }
     if (!(mode & kScanOnly)) {
+      if (vec) {
 #pragma unroll
-      for (int k = 0; k < kEsItems; ++k)
-        if (j0 + k < n) ec_out[j0 + k] = v[k];
+        for (int q = 0; q < kEsItems / 4; ++q)
+          *reinterpret_cast<int4*>(ec_out + j0 + 4 * q) =
+              make_int4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < kEsItems; ++k)
+          if (j0 + k < n) ec_out[j0 + k] = v[k];
+      }
       return;
+    }
+  } else if (vec) {
+#pragma unroll
+    for (int q = 0; q < kEsItems / 4; ++q) {
+      const int4 t = *reinterpret_cast<const int4*>(ec_out + j0 + 4 * q);
+      v[4 * q] = t.x;
+      v[4 * q + 1] = t.y;
+      v[4 * q + 2] = t.z;
+      v[4 * q + 3] = t.w;
     }
   } else {
 #pragma unroll
@@ -193,20 +251,42 @@ __global__ void __launch_bounds__(kEsThreads)
 #pragma unroll
   for (int k = 0; k < kEsItems; ++k) sum += (uint32_t)v[k];
   const uint32_t off = block_exclusive_sum<kEsThreads>(sum, s_warp, &s_misc[2]);
-  if (tid == 0) s_misc[3] = lookback_u32(lb, tile, s_misc[2], status);
+  if (tid < 32) {
+    const uint32_t e = warp_lookback_u32(lb, tile, s_misc[2], status);
+    if (tid == 0) s_misc[3] = e;
+  }
   __syncthreads();
   uint32_t run = s_misc[3] + off;
   int mx = 0;
+  int ps[kEsItems];
 #pragma unroll
   for (int k = 0; k < kEsItems; ++k) {
     const int i = j0 + k;
     run += (uint32_t)v[k];
+    ps[k] = (int)run;
     if (i < n) {
-      if (mode == kEdgeAndScan) ec_out[i] = v[k];
-      ps_out[i] = (int)run;
       const int last = v[k] > 0 ? (int)run + v[k] - 1 : (int)run;
       if (i > 0 && v[k] > 0 && last > mx) mx = last;
       if (i == n - 1 && (int)run > mx) mx = (int)run;
+    }
+  }
+  if (vec) {
+#pragma unroll
+    for (int q = 0; q < kEsItems / 4; ++q) {
+      if (mode == kEdgeAndScan)
+        *reinterpret_cast<int4*>(ec_out + j0 + 4 * q) =
+            make_int4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      *reinterpret_cast<int4*>(ps_out + j0 + 4 * q) =
+          make_int4(ps[4 * q], ps[4 * q + 1], ps[4 * q + 2], ps[4 * q + 3]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kEsItems; ++k) {
+      const int i = j0 + k;
+      if (i < n) {
+        if (mode == kEdgeAndScan) ec_out[i] = v[k];
+        ps_out[i] = ps[k];
+      }
     }
   }
   if (d_max_slot) {

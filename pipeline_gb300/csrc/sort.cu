@@ -147,7 +147,7 @@ struct PassSmem {
 };
 
 template <int RB, int WARPS, int ITEMS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, 2)
     onesweep_pass_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int n,
                          int shift, const uint32_t* __restrict__ bin_base,
                          uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter,
@@ -197,7 +197,12 @@ __global__ void __launch_bounds__(WARPS * 32)
 
   // Per-digit: exclusive offsets across warps, tile count, publish.
   const int invalid = TILE - valid;
-  for (int b = tid; b < BINS; b += THREADS) {
+  constexpr int PER_T = (BINS + THREADS - 1) / THREADS;
+  uint32_t own[PER_T];
+#pragma unroll
+  for (int j = 0; j < PER_T; ++j) {
+    const int b = tid + j * THREADS;
+    if (b >= BINS) break;
     uint32_t run = 0;
 #pragma unroll
     for (int w = 0; w < WARPS; ++w) {
@@ -206,8 +211,8 @@ __global__ void __launch_bounds__(WARPS * 32)
       run += c;
     }
     bin_local[b] = run;  // tile count including out-of-range padding keys
-    const uint32_t cnt = run - (b == (int)MASK ? (uint32_t)invalid : 0u);
-    st_release_u32(lookback + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | cnt);
+    own[j] = run - (b == (int)MASK ? (uint32_t)invalid : 0u);
+    st_release_u32(lookback + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | own[j]);
   }
   __syncthreads();
 
@@ -232,29 +237,68 @@ __global__ void __launch_bounds__(WARPS * 32)
   }
   __syncthreads();
 
-  // Decoupled look-back per digit (bounded waits).
-  for (int b = tid; b < BINS; b += THREADS) {
+  // Decoupled look-back per digit (bounded waits). The first probe reads the
+  // immediate predecessor; past it, a thread loads a window of kWin
+  // predecessor words at once (relaxed loads: flag and count share a word),
+  // so walking back over k tiles that are not yet inclusive costs about
+  // k / kWin round trips. Tiles that start together (the first wave) walk
+  // far; later tiles usually stop at the first probe.
+  constexpr int kWin = 16;
+#pragma unroll
+  for (int j = 0; j < PER_T; ++j) {
+    const int b = tid + j * THREADS;
+    if (b >= BINS) break;
     uint32_t prefix = 0;
-    const uint32_t own = ld_acquire_u32(lookback + (size_t)tile * BINS + b) & kValMask;
     if (tile > 0) {
       int pred = tile - 1;
       uint32_t spins = 0;
-      while (pred >= 0) {
-        const uint32_t w = ld_acquire_u32(lookback + (size_t)pred * BINS + b);
-        const uint32_t f = w & kFlagMask;
-        if (f == 0) {
+      bool done = false;
+      {  // first probe: the immediate predecessor
+        uint32_t w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
+        while ((w0 & kFlagMask) == 0) {
           if (++spins > kSpinLimit) {
             raise_status(status, kStatusSpinTimeout);
             break;
           }
           backoff(spins);
-          continue;
+          w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
         }
-        prefix += w & kValMask;
-        if (f == kFlagInc) break;
+        prefix += w0 & kValMask;
+        done = (w0 & kFlagMask) == kFlagInc || spins > kSpinLimit;
         --pred;
       }
-      st_release_u32(lookback + (size_t)tile * BINS + b, kFlagInc | ((prefix + own) & kValMask));
+      while (!done) {
+        uint32_t w[kWin];
+#pragma unroll
+        for (int k = 0; k < kWin; ++k)
+          w[k] = (pred - k >= 0) ? ld_relaxed_u32(lookback + (size_t)(pred - k) * BINS + b)
+                                 : kFlagInc;
+        bool stop = false;
+        int adv = 0;
+#pragma unroll
+        for (int k = 0; k < kWin; ++k) {
+          const uint32_t f = w[k] & kFlagMask;
+          if (!stop) {
+            if (f == 0) {
+              stop = true;
+            } else {
+              prefix += w[k] & kValMask;
+              ++adv;
+              if (f == kFlagInc) stop = done = true;
+            }
+          }
+        }
+        if (done) break;
+        pred -= adv;
+        if (adv < kWin) {  // stopped at a word that is not ready yet: poll it again
+          if (++spins > kSpinLimit) {
+            raise_status(status, kStatusSpinTimeout);
+            break;
+          }
+          backoff(spins);
+        }
+      }
+      st_release_u32(lookback + (size_t)tile * BINS + b, kFlagInc | ((prefix + own[j]) & kValMask));
     }
     bin_glob[b] = bin_base[b] + prefix - bin_local[b];
   }
