@@ -319,9 +319,45 @@ def run_ours(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     assert int(counts_h[2]) == m
-    e2e = {"value": n * world / (e2e_ms / 1e3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": n * 16,
-           "d2h_bytes_per_step": m * 60 + 16, "ms_per_step": round(e2e_ms, 4)}
+    serial_mpts = n * world / (e2e_ms / 1e3) / 1e6
 
+    # Pipelined through the same public API: three streams, three slots; every
+    # step still uploads its points and downloads its OctNodes + counts.
+    from pipeline_gb300.pipeline import PipelinedBuilder
+
+    del builder
+    torch.cuda.empty_cache()
+    pb = PipelinedBuilder(n, depth=3, device=dev)
+    outs = [torch.empty((m, 15), dtype=torch.int32).pin_memory() for _ in range(3)]
+    frames = [(pinned, MIN_COORD, RANGE)] * e2e_steps
+    pb.run(frames[:3], outs)
+    pb.synchronize()
+    barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(pb.s_up)
+    res = pb.run(frames, outs)
+    t_end.record(pb.s_down)
+    t_end.synchronize()
+    pipe_ms = t_start.elapsed_time(t_end) / e2e_steps
+    if world > 1:
+        t = torch.tensor([pipe_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        pipe_ms = float(t.item())
+    assert all(r[2] == m and r[3] == 0 for r in res)
+    e2e = {"value": n * world / (pipe_ms / 1e3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+           "d2h_bytes_per_step": m * 60 + 16, "ms_per_step": round(pipe_ms, 4),
+           "mode": "pipelined: upload, build and download of consecutive steps overlap "
+                   "(3 streams, 3 slots)",
+           "serial_value": round(serial_mpts, 2), "serial_ms_per_step": round(e2e_ms, 4)}
+    del pb, outs
+
+    workloads = {}
+    if not args.no_extra:
+        torch.cuda.empty_cache()
+        workloads["clustered_16m"] = clustered_workload(dev, flush, max(5, min(args.steps, 20)))
+        torch.cuda.empty_cache()
+        workloads["batched_512"] = batched_workload(dev, flush, max(5, min(args.steps, 20)))
     if rank != 0:
         return 0
     base = None
@@ -339,7 +375,7 @@ def run_ours(args, rank, world, local_rank):
                    "wall_s_timed_region": round(t_wall, 3)},
         "roofline": roofline, "stages": stages, "e2e": e2e,
         "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-        "cpu_baseline": base,
+        "cpu_baseline": base, "workloads": workloads,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -361,6 +397,115 @@ def profile_only(args):
     c = b.counts()
     print(f"profile build: U={c.n_unique} M={c.n_oct} status={c.status}")
     return 0 if c.status == 0 else 1
+
+
+def _time_events(fn, reps, stream, flush):
+    import torch
+
+    ts = []
+    for r in range(reps):
+        flush.fill_(r & 0xFF)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def clustered_workload(dev, flush, reps):
+    """16,777,216-point clustered cloud: learned bucketed sort vs plain."""
+    import torch
+
+    from pipeline_gb300 import datasets
+    from pipeline_gb300.kernels import k_ComputeMortonCode
+    from pipeline_gb300.learned import LearnedCDF
+    from pipeline_gb300.pipeline import LearnedOctreeBuilder, OctreeBuilder
+
+    n = N_POINTS
+    pts_h = datasets.clustered(n, seed=7)
+    pts = torch.from_numpy(pts_h).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    # the model is fit on Morton codes the pipeline produced for a sample of points
+    idx = torch.from_numpy(np.random.default_rng(1).integers(0, n, 1 << 18)).to(dev)
+    sample_pts = pts.index_select(0, idx).contiguous()
+    sample_keys = torch.empty(1 << 18, dtype=torch.int32, device=dev)
+    k_ComputeMortonCode(sample_pts, sample_keys, 1 << 18, MIN_COORD, RANGE)
+    model = LearnedCDF(max_segments=4096)
+    t0 = time.perf_counter()
+    model.fit(sample_keys, n_segments=4096, steps=100, lr=0.05, n_buckets=4096)
+    torch.cuda.synchronize(dev)
+    fit_ms = (time.perf_counter() - t0) * 1e3
+    plain = OctreeBuilder(n, device=dev)
+    learned = LearnedOctreeBuilder(n, model, device=dev)
+    for _ in range(3):
+        plain.build(pts, MIN_COORD, RANGE)
+        learned.build(pts, MIN_COORD, RANGE)
+    torch.cuda.synchronize(dev)
+    pc, lc = plain.counts(), learned.counts()
+    exact = (pc.n_unique, pc.n_oct) == (lc.n_unique, lc.n_oct) and torch.equal(
+        plain.nodes[: pc.n_oct], learned.nodes[: lc.n_oct]) and torch.equal(
+        plain.codes[: pc.n_unique], learned.codes[: lc.n_unique])
+    t_plain = _time_events(lambda: plain.build(pts, MIN_COORD, RANGE), reps, stream, flush)
+    t_learned = _time_events(lambda: learned.build(pts, MIN_COORD, RANGE), reps, stream, flush)
+    st = learned.lsort_stats()
+    h = model.header()
+    return {"workload": "clustered_16m: 64 anisotropic Gaussians (sigma 0.5-20% of the box) + 5% "
+                        "uniform noise, 16,777,216 points, seed 7",
+            "n_unique": pc.n_unique, "plain_mpts": round(n / t_plain / 1e3, 1),
+            "learned_mpts": round(n / t_learned / 1e3, 1),
+            "speedup": round(t_plain / t_learned, 3), "bit_exact": bool(exact),
+            "overflow_frac": round(st["overflow_frac"], 5), "fallback": st["fallback"],
+            "max_bucket": st["max_bucket"], "fit_loss": h["loss"], "fit_ms": round(fit_ms, 2),
+            "fit": "4096 segments, 262,144 sampled Morton codes, 100 Adam steps"}
+
+
+def batched_workload(dev, flush, reps):
+    """512 clouds (log-uniform 1K-1M points): one batched sequence vs a
+    per-cloud plain loop."""
+    import torch
+
+    from pipeline_gb300 import datasets
+    from pipeline_gb300.batch import BatchOctreeBuilder
+    from pipeline_gb300.pipeline import OctreeBuilder
+
+    clouds = datasets.batched(512, seed=11)
+    sizes = [len(c) for c in clouds]
+    total = int(sum(sizes))
+    stream = torch.cuda.current_stream(dev)
+    pts = torch.from_numpy(np.concatenate(clouds, 0)).to(dev)
+    mins = torch.zeros(len(clouds), dtype=torch.float32, device=dev)
+    ranges = torch.full((len(clouds),), RANGE, dtype=torch.float32, device=dev)
+    b = BatchOctreeBuilder(sizes, device=dev)
+    b.capture(pts, mins, ranges)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    single = OctreeBuilder(max(sizes), device=dev)
+    views = [pts[offs[c]:offs[c + 1]] for c in range(len(clouds))]
+
+    def loop():
+        for v in views:
+            single.build(v, MIN_COORD, RANGE)
+
+    loop()
+    b.replay()
+    torch.cuda.synchronize(dev)
+    # bit-exactness spot check against the per-cloud build
+    counts = b.cloud_counts()
+    exact = True
+    for c in range(0, 512, 51):
+        single.build(views[c], MIN_COORD, RANGE)
+        r = single.result()
+        g = b.cloud_result(c, counts)
+        exact &= r["oct_nodes"].tobytes() == g["oct_nodes"].tobytes()
+    t_batch = _time_events(b.replay, reps, stream, flush)
+    t_loop = _time_events(loop, max(2, reps // 4), stream, flush)
+    return {"workload": "batched_512: 512 clouds, sizes log-uniform in [1K, 1M] (seed 11), even "
+                        "uniform, odd 8-Gaussian mixtures; one CUDA-graph-captured batched build",
+            "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
+            "per_cloud_loop_mpts": round(total / t_loop / 1e3, 1),
+            "speedup": round(t_loop / t_batch, 3), "bit_exact_spot_check": bool(exact)}
 
 
 def read_traffic(kernel_step: str, n: int):
@@ -385,6 +530,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the clustered (learned) and batched workloads")
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up builds plus one build, no timing or output (for ncu captures)")
     ap.add_argument("--points", type=int, default=N_POINTS,

@@ -251,6 +251,96 @@ OCT_API int oct_build_octree_timed(const oct_vec4* points, int n, float min_coor
                                    size_t workspace_bytes, void* const* events, int n_events,
                                    oct_stream_t stream);
 
+/* ----------------------------------------------------------------------- */
+/* Learned CDF of the Morton-key distribution (the learned-sort extension;   */
+/* no counterpart in the reference). A model lives in one device buffer: a   */
+/* 256-byte versioned header plus arrays laid out for max_segments (<= 4096);*/
+/* copying the buffer persists the model. Model: monotone piecewise-linear   */
+/* CDF, knots at evenly spaced ranks of a sorted key sample, heights         */
+/* y_k = cumsum(softplus(theta)) / sum(softplus(theta)), trained by Adam on  */
+/* the mean squared error against the sample's empirical CDF. Bucket ids     */
+/* come from exact fixed-point tables and never decrease with the key.       */
+/* ----------------------------------------------------------------------- */
+#define OCT_LCDF_MAX_SEGMENTS 4096
+/* Byte offsets of the model's parts: {x, theta, adam_m, adam_v, y, grad, yq,
+ * slope, lut, total}; x is uint32[K+1], theta/adam/y/grad float, yq uint32[K+1],
+ * slope uint64[K], lut uint32[4097]. */
+OCT_API int oct_lcdf_layout(int max_segments, size_t offsets[10]);
+OCT_API size_t oct_lcdf_fit_workspace_bytes(int n_sample);
+/* Sorts the sample into the workspace, places knots, runs `steps` Adam steps
+ * (learning rate lr) and builds bucket tables for n_buckets (<= 65536). */
+OCT_API int oct_lcdf_fit(const uint32_t* sample_keys, int n_sample, int n_segments, int steps,
+                         float lr, int n_buckets, void* model, int max_segments,
+                         void* workspace, size_t workspace_bytes, oct_stream_t stream);
+/* Loss (written into the header) and dL/dtheta (d_grad, K floats) of the
+ * model's current theta on a SORTED sample. */
+OCT_API int oct_lcdf_loss_grad(const uint32_t* sorted_sample, int n_sample, void* model,
+                               int max_segments, float* d_grad, oct_stream_t stream);
+/* `steps` more Adam steps (learning rate lr) on the model's current theta. */
+OCT_API int oct_lcdf_train_steps(const uint32_t* sorted_sample, int n_sample, void* model,
+                                 int max_segments, int steps, float lr, oct_stream_t stream);
+/* Rebuild the bucket tables from the current theta for n_buckets. */
+OCT_API int oct_lcdf_tables(void* model, int max_segments, int n_buckets, oct_stream_t stream);
+/* d_buckets[i] = bucket of keys[i] (30-bit keys). */
+OCT_API int oct_lcdf_buckets(const void* model, int max_segments, const uint32_t* keys, int n,
+                             uint32_t* d_buckets, oct_stream_t stream);
+
+/* Learned bucketed sort + unique: sorted unique keys of keys[0, n) (30-bit)
+ * into out_unique and U into *d_n_unique, through `model` (tables built for
+ * n_buckets). Keys are scattered into model buckets and each bucket is sorted
+ * and de-duplicated in shared memory; when more than overflow_threshold of the
+ * keys sit in oversized buckets, or a bucket fits no shared-memory form, the
+ * same launches fall back to the OneSweep sort + unique (device-side switch).
+ * d_stats (nullable, 32 bytes): {fallback, failed_buckets, overflow_keys,
+ * max_bucket, n, overflow_frac (float), skip, 0}. On the fallback path `keys`
+ * is sorted in place; otherwise it is left as it was. */
+OCT_API size_t oct_lsort_workspace_bytes(int n, int n_buckets, int max_segments);
+OCT_API int oct_lsort_unique(uint32_t* keys, int n, const void* model, int max_segments,
+                             int n_buckets, float overflow_threshold, uint32_t* out_unique,
+                             int32_t* d_n_unique, void* d_stats, void* workspace,
+                             size_t workspace_bytes, uint32_t* d_status, oct_stream_t stream);
+/* Whole build with the learned sort for stages 2-3 (outputs as oct_build_octree). */
+OCT_API size_t oct_build_learned_workspace_bytes(int n, int nodes_capacity, int n_buckets,
+                                                 int max_segments);
+OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_coord, float range,
+                                     const void* model, int max_segments, int n_buckets,
+                                     float overflow_threshold, const oct_build_outputs* out,
+                                     void* d_stats, void* workspace, size_t workspace_bytes,
+                                     oct_stream_t stream);
+/* Radix sort shape used by sort plans made after the call (the autotuner's
+ * knob): radix_bits 10 or 8, warps 16, items 16 or 24, scan 0 (decoupled
+ * look-back) or 1 (per-tile histograms + tile scan). */
+OCT_API int oct_set_sort_config(int radix_bits, int warps, int items, int scan);
+OCT_API int oct_get_sort_config(int out[4]);
+
+/* ----------------------------------------------------------------------- */
+/* Batched build: many clouds of uneven size in one launch sequence (the     */
+/* batched-build extension; no counterpart in the reference, whose drivers   */
+/* build one cloud per run). Points of all clouds are concatenated; cloud c  */
+/* owns points / codes / tree arrays / edge counts / prefix sums at          */
+/* [start_c, start_c + n_c) and OctNodes at [node_start_c, node_start_c +    */
+/* cap_c). Each cloud's outputs are bit-identical to oct_build_octree on it. */
+/* The plan (a host object) fixes the cloud sizes and the sort shape; its    */
+/* device tables are uploaded once; builds are capturable in CUDA graphs.    */
+/* d_cloud_counts: int32[4 * n_clouds] = per cloud {U, U-1, M, status}.     */
+/* ----------------------------------------------------------------------- */
+typedef struct oct_batch_plan oct_batch_plan;
+/* h_node_caps may be NULL (cap_c = n_c). Returns NULL on bad sizes. */
+OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_cloud_sizes,
+                                              const int32_t* h_node_caps);
+OCT_API void oct_batch_plan_destroy(oct_batch_plan* plan);
+/* {n_clouds, total points, total OctNode capacity, table bytes, workspace
+ * bytes, sort tiles} */
+OCT_API int oct_batch_plan_info(const oct_batch_plan* plan, int64_t out[6]);
+/* Copies the plan's tables into d_tables (256-byte aligned, table bytes). */
+OCT_API int oct_batch_upload_tables(const oct_batch_plan* plan, void* d_tables,
+                                    oct_stream_t stream);
+OCT_API int oct_build_octree_batch(const oct_batch_plan* plan, const void* d_tables,
+                                   const oct_vec4* points, const float* d_mins,
+                                   const float* d_ranges, const oct_build_outputs* out,
+                                   int32_t* d_cloud_counts, void* workspace,
+                                   size_t workspace_bytes, oct_stream_t stream);
+
 /* Synchronous convenience: copies d_counts to the host after the stream
  * drains and maps the status word to OCT_ERR_DEVICE / OCT_ERR_CAPACITY. */
 OCT_API int oct_read_counts(const int32_t* d_counts, int32_t* h_counts, oct_stream_t stream);

@@ -94,6 +94,24 @@ SIGNATURES = {
     "oct_build_workspace_bytes": (Z, [I, I]),
     "oct_build_octree": (I, [P, I, F, F, C.POINTER(OctBuildOutputs), P, Z, P]),
     "oct_read_counts": (I, [P, P, P]),
+    "oct_lcdf_layout": (I, [I, P]),
+    "oct_lcdf_fit_workspace_bytes": (Z, [I]),
+    "oct_lcdf_fit": (I, [P, I, I, I, F, I, P, I, P, Z, P]),
+    "oct_lcdf_loss_grad": (I, [P, I, P, I, P, P]),
+    "oct_lcdf_tables": (I, [P, I, I, P]),
+    "oct_lcdf_train_steps": (I, [P, I, P, I, I, F, P]),
+    "oct_lcdf_buckets": (I, [P, I, P, I, P, P]),
+    "oct_lsort_workspace_bytes": (Z, [I, I, I]),
+    "oct_lsort_unique": (I, [P, I, P, I, I, F, P, P, P, P, Z, P, P]),
+    "oct_build_learned_workspace_bytes": (Z, [I, I, I, I]),
+    "oct_build_octree_learned": (I, [P, I, F, F, P, I, I, F, C.POINTER(OctBuildOutputs), P, P, Z, P]),
+    "oct_set_sort_config": (I, [I, I, I, I]),
+    "oct_get_sort_config": (I, [P]),
+    "oct_batch_plan_create": (P, [I, P, P]),
+    "oct_batch_plan_destroy": (None, [P]),
+    "oct_batch_plan_info": (I, [P, P]),
+    "oct_batch_upload_tables": (I, [P, P, P]),
+    "oct_build_octree_batch": (I, [P, P, P, P, P, C.POINTER(OctBuildOutputs), P, P, Z, P]),
     "oct_build_step_count": (I, []),
     "oct_build_step_name": (C.c_char_p, [I]),
     "oct_build_octree_timed": (I, [P, I, F, F, C.POINTER(OctBuildOutputs), P, Z, P, I, P]),

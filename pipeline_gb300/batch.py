@@ -1,0 +1,124 @@
+"""Batched octree build: many clouds of uneven size in one launch sequence.
+
+``BatchOctreeBuilder(sizes)`` plans the batch once (tile descriptors, cloud
+offsets, workspace), then ``build(points, mins, ranges)`` builds every cloud;
+``capture()``/``replay()`` run the same launches as one CUDA graph.
+``shard_clouds`` splits a batch over ranks (independent clouds: no
+collective is needed).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .kernels import OCTNODE_WORDS, oct_nodes_to_numpy
+
+
+def shard_clouds(sizes, world: int) -> list[list[int]]:
+    """Greedy longest-first assignment of clouds to `world` ranks by point
+    count (each cloud to the currently lightest rank; ties to the lower rank).
+    Deterministic; every cloud appears on exactly one rank."""
+    order = sorted(range(len(sizes)), key=lambda c: (-int(sizes[c]), c))
+    loads = [0] * world
+    out: list[list[int]] = [[] for _ in range(world)]
+    for c in order:
+        r = min(range(world), key=lambda k: (loads[k], k))
+        out[r].append(c)
+        loads[r] += int(sizes[c])
+    return [sorted(x) for x in out]
+
+
+class BatchOctreeBuilder:
+    def __init__(self, sizes, node_caps=None, device="cuda"):
+        self.lib = _lib.load()
+        self.device = torch.device(device)
+        self.sizes = np.asarray(sizes, np.int32)
+        caps = None if node_caps is None else np.asarray(node_caps, np.int32)
+        self.plan = self.lib.oct_batch_plan_create(
+            len(self.sizes), self.sizes.ctypes.data, None if caps is None else caps.ctypes.data)
+        if not self.plan:
+            raise ValueError("oct_batch_plan_create rejected the cloud sizes")
+        info = (C.c_int64 * 6)()
+        _lib.check(self.lib.oct_batch_plan_info(self.plan, info), "oct_batch_plan_info")
+        self.n_clouds, self.n, self.cap, tbytes, wbytes, self.sort_tiles = (int(v) for v in info)
+        self.start = np.concatenate([[0], np.cumsum(self.sizes.astype(np.int64))]).astype(np.int64)
+        cap_arr = self.sizes if caps is None else caps
+        self.node_start = np.concatenate([[0], np.cumsum(cap_arr.astype(np.int64))]).astype(np.int64)
+        dev = self.device
+        n = max(self.n, 1)
+        self.tables = torch.empty(max(tbytes, 256), dtype=torch.uint8, device=dev)
+        self.workspace = torch.empty(max(wbytes, 256), dtype=torch.uint8, device=dev)
+        self.codes = torch.empty(n, dtype=torch.int32, device=dev)
+        self.prefix_n = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.has_leaf_left = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.has_leaf_right = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.left_child = torch.empty(n, dtype=torch.int32, device=dev)
+        self.parent = torch.empty(n, dtype=torch.int32, device=dev)
+        self.edge_count = torch.empty(n, dtype=torch.int32, device=dev)
+        self.prefix_sum = torch.empty(n, dtype=torch.int32, device=dev)
+        self.nodes = torch.empty((max(self.cap, 1), OCTNODE_WORDS), dtype=torch.int32, device=dev)
+        self.counts = torch.zeros(4 * self.n_clouds, dtype=torch.int32, device=dev)
+        self._out = _lib.OctBuildOutputs(
+            codes=self.codes.data_ptr(), n_nodes=0, prefix_n=self.prefix_n.data_ptr(),
+            has_leaf_left=self.has_leaf_left.data_ptr(), has_leaf_right=self.has_leaf_right.data_ptr(),
+            left_child=self.left_child.data_ptr(), parent=self.parent.data_ptr(),
+            edge_count=self.edge_count.data_ptr(), prefix_sum=self.prefix_sum.data_ptr(),
+            nodes=self.nodes.data_ptr(), nodes_capacity=max(self.cap, 1), d_counts=self.counts.data_ptr())
+        s = torch.cuda.current_stream(dev)
+        _lib.check(self.lib.oct_batch_upload_tables(self.plan, C.c_void_p(self.tables.data_ptr()),
+                                                     C.c_void_p(s.cuda_stream)), "oct_batch_upload_tables")
+        self._graph = None
+
+    def __del__(self):
+        try:
+            if getattr(self, "plan", None):
+                self.lib.oct_batch_plan_destroy(self.plan)
+                self.plan = None
+        except Exception:
+            pass
+
+    def build(self, points: torch.Tensor, mins: torch.Tensor, ranges: torch.Tensor,
+              stream: torch.cuda.Stream | None = None) -> None:
+        if points.numel() < 4 * self.n or not points.is_cuda or points.dtype != torch.float32:
+            raise ValueError("points: float32 CUDA tensor of the batch's total size x 4")
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        rc = self.lib.oct_build_octree_batch(
+            self.plan, C.c_void_p(self.tables.data_ptr()), C.c_void_p(points.data_ptr()),
+            C.c_void_p(mins.data_ptr()), C.c_void_p(ranges.data_ptr()), C.byref(self._out),
+            C.c_void_p(self.counts.data_ptr()), C.c_void_p(self.workspace.data_ptr()),
+            self.workspace.numel(), C.c_void_p(s.cuda_stream))
+        _lib.check(rc, "oct_build_octree_batch")
+
+    def capture(self, points, mins, ranges):
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self.build(points, mins, ranges)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        torch.cuda.synchronize(self.device)
+        with torch.cuda.graph(g):
+            self.build(points, mins, ranges)
+        self._graph = g
+        return g
+
+    def replay(self):
+        self._graph.replay()
+
+    def cloud_counts(self) -> np.ndarray:
+        return self.counts.cpu().numpy().reshape(-1, 4)
+
+    def cloud_result(self, c: int, counts: np.ndarray | None = None) -> dict:
+        cnt = self.cloud_counts() if counts is None else counts
+        u, b, m, st = (int(x) for x in cnt[c])
+        cs, ns = int(self.start[c]), int(self.node_start[c])
+        out = {"n_unique": u, "n_brt": b, "n_oct": m, "status": st & 0xFFFFFFFF,
+               "sorted_unique": self.codes[cs:cs + u].cpu().numpy().view(np.uint32)}
+        for name in ("prefix_n", "has_leaf_left", "has_leaf_right", "left_child", "parent",
+                     "edge_count", "prefix_sum"):
+            out[name] = getattr(self, name)[cs:cs + b].cpu().numpy()
+        out["oct_nodes"] = oct_nodes_to_numpy(self.nodes[ns:ns + m]) if m else np.zeros(0)
+        return out

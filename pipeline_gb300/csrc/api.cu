@@ -41,12 +41,15 @@ BuildLayout build_layout(int n, int cap) {
   L.sort = sort_plan(n, 30);
   L.uniq = unique_plan(n);
   L.scan = edge_scan_plan(n);
-  L.sort_off = 0;
-  L.uniq_off = align_up(L.sort_off + L.sort.bytes, 256);
+  // Everything that must start at zero is contiguous from offset 0 up to the
+  // end of the sort's zeroed part; the sort's digit bases and per-tile
+  // histograms (always fully written before use) follow.
+  L.uniq_off = 0;
   L.scan_off = align_up(L.uniq_off + L.uniq.bytes, 256);
   L.misc_off = align_up(L.scan_off + L.scan.bytes, 256);
-  L.ctrl_bytes = align_up(L.misc_off + 256, 256);
-  L.keys_a_off = L.ctrl_bytes;
+  L.sort_off = align_up(L.misc_off + 256, 256);
+  L.ctrl_bytes = L.sort_off + L.sort.zero_bytes;
+  L.keys_a_off = align_up(L.sort_off + L.sort.bytes, 256);
   L.keys_b_off = align_up(L.keys_a_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
   L.tags_off = align_up(L.keys_b_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
   L.total = align_up(L.tags_off + oct_tags_bytes(cap), 256);
@@ -145,7 +148,7 @@ int oct_sort_keys(uint32_t* keys, uint32_t* keys_alt, int n, int key_bits, void*
   const SortPlan p = sort_plan(n, key_bits);
   if (workspace_bytes < p.bytes) return OCT_ERR_WORKSPACE;
   cudaStream_t s = S(stream);
-  OCT_TRY(cudaMemsetAsync(workspace, 0, p.bytes, s), "oct_sort_keys: clear");
+  OCT_TRY(cudaMemsetAsync(workspace, 0, p.zero_bytes, s), "oct_sort_keys: clear");
   OCT_TRY(launch_histogram(keys, &p, workspace, s), "oct_sort_keys: histogram");
   uint32_t* result = keys;
   OCT_TRY(launch_sort_passes(keys, keys_alt, &p, workspace, d_status, s, &result),

@@ -1,0 +1,760 @@
+// Batched build: many point clouds of uneven size in one launch sequence.
+//
+// The clouds are concatenated (cloud c holds points [start_c, start_c + n_c));
+// every output array keeps that layout, so cloud c's codes, tree arrays,
+// edge counts and prefix sums start at start_c and its OctNodes at
+// node_start_c. Each cloud is built exactly as a single build of it would be
+// (bit-identical), but every stage runs for all clouds in one launch:
+//
+//   morton    tiles never cross clouds; each CTA walks a contiguous run of
+//             tiles and flushes its shared digit histograms per cloud;
+//   sort      reduce-then-scan radix passes: per-tile digit histograms, a
+//             per-cloud tile-prefix scan, and the pass kernel driven by tile
+//             descriptors (cloud-local positions are absolute indices);
+//   unique,   decoupled look-back chains that restart at each cloud's first
+//   scan      tile; tiles come from an atomic work queue;
+//   tree,     one thread per global node / slot, mapped to its cloud by a
+//   octree    binary search over the cloud starts, reusing the single-cloud
+//             node and slot functions on per-cloud views.
+//
+// The host plan (tile descriptors, cloud starts) is uploaded once; every
+// size that depends on the data (U_c, M_c) stays on the device, so a batch
+// build is a fixed launch sequence that CUDA graphs capture.
+#include <stdio.h>
+
+#include <new>
+#include <vector>
+
+#include "octree.cuh"
+#include "tree.cuh"
+
+namespace octgb {
+
+constexpr int kBatchTile4k = 4096;  // unique / scan tiles (keys or nodes)
+
+// ---------------------------------------------------------------- helpers --
+// Cloud of global index g: largest c with start[c] <= g (start[C] = total).
+__device__ __forceinline__ int cloud_of(const int* __restrict__ start, int C, int g) {
+  int lo = 0, hi = C - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(start + mid) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct BatchDev {
+  int C;
+  int N;
+  const int* start;       // [C+1] point starts
+  const int* node_start;  // [C+1] OctNode starts
+  const float* mins;      // [C]
+  const float* ranges;    // [C]
+  const int4* sort_tiles; // [Ts]
+  int Ts;
+  const int* cloud_tile0; // [C+1] first sort tile of each cloud
+  const int4* tiles4k;    // [T4] {first, end, cloud, first tile of cloud}
+  int T4;
+};
+
+// ------------------------------------------------------------------ morton --
+template <int RB>
+__global__ void __launch_bounds__(256)
+    batch_morton_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, BatchDev B,
+                        uint32_t* __restrict__ ghist, int passes, uint32_t* __restrict__ status) {
+  constexpr int BINS = 1 << RB;
+  extern __shared__ uint32_t s_hist[];
+  const int t0 = (int)((long long)B.Ts * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)B.Ts * (blockIdx.x + 1) / gridDim.x);
+  for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x) s_hist[i] = 0;
+  __syncthreads();
+  bool bad = false;
+  int cur = t0 < t1 ? B.sort_tiles[t0].z : -1;
+  for (int t = t0; t < t1; ++t) {
+    const int4 d = B.sort_tiles[t];
+    if (d.z != cur) {  // flush the previous cloud's histograms
+      __syncthreads();
+      uint32_t* g = ghist + (size_t)cur * passes * BINS;
+      for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x) {
+        if (s_hist[i]) atomicAdd(&g[i], s_hist[i]);
+        s_hist[i] = 0;
+      }
+      __syncthreads();
+      cur = d.z;
+    }
+    const float mn = B.mins[d.z], rg = B.ranges[d.z];
+    for (int i = d.x + threadIdx.x; i < d.y; i += blockDim.x) {
+      const float4 p = ld_stream_f4(pts + i);
+      bad |= !(in_range(p.x, mn, rg) && in_range(p.y, mn, rg) && in_range(p.z, mn, rg));
+      const uint32_t c = morton_code(p.x, p.y, p.z, mn, rg);
+      keys[i] = c;
+      for (int ps = 0; ps < passes; ++ps)
+        atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);
+    }
+  }
+  __syncthreads();
+  if (cur >= 0) {
+    uint32_t* g = ghist + (size_t)cur * passes * BINS;
+    for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x)
+      if (s_hist[i]) atomicAdd(&g[i], s_hist[i]);
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) raise_status(status, kStatusRange);
+}
+
+// base[c][p][d] = start_c + exclusive prefix of cloud c's pass-p histogram.
+template <int RB>
+__global__ void __launch_bounds__(1024)
+    batch_hist_scan_kernel(const uint32_t* __restrict__ ghist, uint32_t* __restrict__ base,
+                           BatchDev B, int passes) {
+  constexpr int BINS = 1 << RB;
+  constexpr int T = BINS < 1024 ? BINS : 1024;
+  constexpr int PER = BINS / T;
+  __shared__ uint32_t warp_tot[32];
+  __shared__ uint32_t total;
+  const int c = blockIdx.x / passes;
+  const uint32_t* h = ghist + (size_t)blockIdx.x * BINS;
+  uint32_t* o = base + (size_t)blockIdx.x * BINS;
+  // launched with exactly T threads (every thread reaches the block scan)
+  uint32_t v[PER];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    v[j] = h[threadIdx.x * PER + j];
+    sum += v[j];
+  }
+  uint32_t ex = block_exclusive_sum<T>(sum, warp_tot, &total) + (uint32_t)B.start[c];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    o[threadIdx.x * PER + j] = ex;
+    ex += v[j];
+  }
+}
+
+// In place: th[t][d] = where tile t's keys of digit d start, for the tiles of
+// cloud blockIdx.x (blocks: clouds x 32-digit groups; 32 digits x 32 tile
+// groups per block).
+__global__ void __launch_bounds__(1024)
+    batch_tile_scan_kernel(uint32_t* __restrict__ th, int bins, const uint32_t* __restrict__ base,
+                           int passes, int pass, BatchDev B) {
+  __shared__ uint32_t part[32][33];
+  const int c = blockIdx.x;
+  const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int d = blockIdx.y * 32 + l;
+  const int ta = B.cloud_tile0[c], tb = B.cloud_tile0[c + 1];
+  const int nt = tb - ta;
+  const int t0 = ta + (int)((long long)nt * g / 32), t1 = ta + (int)((long long)nt * (g + 1) / 32);
+  uint32_t sum = 0;
+  if (d < bins)
+    for (int t = t0; t < t1; ++t) sum += th[(size_t)t * bins + d];
+  part[g][l] = sum;
+  __syncthreads();
+  if (d >= bins) return;
+  uint32_t run = base[((size_t)c * passes + pass) * bins + d];
+  for (int k = 0; k < g; ++k) run += part[k][l];
+  for (int t = t0; t < t1; ++t) {
+    const uint32_t v = th[(size_t)t * bins + d];
+    th[(size_t)t * bins + d] = run;
+    run += v;
+  }
+}
+
+// ------------------------------------------------------ look-back chains --
+constexpr unsigned long long kBAgg = 1ull << 62;
+constexpr unsigned long long kBInc = 2ull << 62;
+constexpr unsigned long long kBFlags = 3ull << 62;
+
+// Warp look-back whose chain starts at tile `first` (the cloud's first tile).
+__device__ uint32_t chain_lookback(unsigned long long* lb, int tile, int first, uint32_t agg,
+                                   uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  if (tile == first) {
+    if (lane == 0) st_release_u64(lb + tile, kBInc | agg);
+    return 0;
+  }
+  if (lane == 0) st_release_u64(lb + tile, kBAgg | agg);
+  uint32_t ex = 0;
+  int pred = tile - 1;
+  uint32_t spins = 0;
+  while (true) {
+    const int p = pred - lane;
+    const unsigned long long w = p >= first ? ld_relaxed_u64(lb + p) : kBInc;
+    const unsigned long long f = w & kBFlags;
+    const uint32_t inc_m = __ballot_sync(0xffffffffu, f == kBInc);
+    const uint32_t nr_m = __ballot_sync(0xffffffffu, f == 0);
+    const int first_inc = inc_m ? __ffs(inc_m) - 1 : 32;
+    const int first_nr = nr_m ? __ffs(nr_m) - 1 : 32;
+    if (first_nr < first_inc) {
+      ex += __reduce_add_sync(0xffffffffu, lane < first_nr ? (uint32_t)w : 0u);
+      pred -= first_nr;
+      if (++spins > kSpinLimit) {
+        if (lane == 0) raise_status(status, kStatusSpinTimeout);
+        break;
+      }
+      backoff(spins);
+      continue;
+    }
+    const int take = first_inc < 32 ? first_inc + 1 : 32;
+    ex += __reduce_add_sync(0xffffffffu, lane < take ? (uint32_t)w : 0u);
+    if (first_inc < 32) break;
+    pred -= 32;
+  }
+  if (lane == 0) st_release_u64(lb + tile, kBInc | (uint32_t)(ex + agg));
+  return ex;
+}
+
+__device__ __forceinline__ bool last_tile_of_cloud(const BatchDev& B, int t) {
+  return t == B.T4 - 1 || B.tiles4k[t + 1].z != B.tiles4k[t].z;
+}
+
+// ----------------------------------------------------------------- unique --
+constexpr int kBuThreads = 256;
+constexpr int kBuItems = 16;
+static_assert(kBuThreads * kBuItems == kBatchTile4k, "unique tile");
+
+__device__ __forceinline__ int pad_idx4k(int j) { return j + (j >> 5); }
+
+__global__ void __launch_bounds__(kBuThreads)
+    batch_unique_kernel(const uint32_t* src, uint32_t* dst, BatchDev B, int* __restrict__ unique_c,
+                        unsigned long long* __restrict__ lb, uint32_t* __restrict__ queue,
+                        uint32_t* __restrict__ status) {
+  __shared__ uint32_t s_keys[kBatchTile4k + kBatchTile4k / 32];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_misc[4];
+  const int tid = threadIdx.x;
+  while (true) {
+    if (tid == 0) s_misc[0] = atomicAdd(queue, 1u);
+    __syncthreads();
+    const int t = (int)s_misc[0];
+    if (t >= B.T4) return;
+    const int4 d = B.tiles4k[t];
+    const int start = d.x, valid = d.y - d.x, c = d.z;
+    const int cs = B.start[c];
+#pragma unroll 4
+    for (int j = tid; j < kBatchTile4k; j += kBuThreads)
+      s_keys[pad_idx4k(j)] = j < valid ? src[start + j] : 0u;
+    if (tid == 0) s_misc[1] = start > cs ? src[start - 1] : 0u;
+    __syncthreads();
+    uint32_t key[kBuItems];
+    uint32_t flags = 0;
+    int cnt = 0;
+    const int j0 = tid * kBuItems;
+    uint32_t prev = j0 == 0 ? s_misc[1] : s_keys[pad_idx4k(j0 - 1)];
+#pragma unroll
+    for (int k = 0; k < kBuItems; ++k) {
+      key[k] = s_keys[pad_idx4k(j0 + k)];
+      const int j = j0 + k;
+      const bool head = j < valid && ((start + j == cs) || key[k] != prev);
+      flags |= (uint32_t)head << k;
+      cnt += head;
+      prev = key[k];
+    }
+    const uint32_t off = block_exclusive_sum<kBuThreads>((uint32_t)cnt, s_warp, &s_misc[2]);
+    const uint32_t total = s_misc[2];
+    if (tid < 32) {
+      const uint32_t e = chain_lookback(lb, t, d.w, total, status);
+      if (tid == 0) s_misc[3] = e;
+    }
+    uint32_t o = off;
+#pragma unroll
+    for (int k = 0; k < kBuItems; ++k)
+      if (flags >> k & 1u) s_keys[pad_idx4k(o++)] = key[k];
+    __syncthreads();
+    const uint32_t ex = s_misc[3];
+    for (int j = tid; j < (int)total; j += kBuThreads) dst[cs + ex + j] = s_keys[pad_idx4k(j)];
+    if (tid == 0 && last_tile_of_cloud(B, t)) unique_c[c] = (int)(ex + total);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ radix tree --
+__global__ void __launch_bounds__(256)
+    batch_tree_kernel(const uint32_t* __restrict__ codes, BatchDev B,
+                      const int* __restrict__ unique_c, uint8_t* __restrict__ prefix_n,
+                      uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
+                      int* __restrict__ left_child, int* __restrict__ parent) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < B.N; g += gridDim.x * blockDim.x) {
+    const int c = cloud_of(B.start, B.C, g);
+    const int cs = B.start[c];
+    const int nb = max(unique_c[c] - 1, 0);
+    const int i = g - cs;
+    if (i < nb)
+      radix_node(i, nb, codes + cs, prefix_n + cs, hll + cs, hlr + cs, left_child + cs,
+                 parent + cs);
+  }
+}
+
+// ------------------------------------------------- edge count + prefix sum --
+__global__ void __launch_bounds__(256)
+    batch_edge_scan_kernel(BatchDev B, const int* __restrict__ unique_c,
+                           const uint8_t* __restrict__ prefix_n, const int* __restrict__ parent,
+                           int* __restrict__ ec_out, int* __restrict__ ps_out,
+                           int* __restrict__ max_slot_c, unsigned long long* __restrict__ lb,
+                           uint32_t* __restrict__ queue, uint32_t* __restrict__ status) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_misc[4];
+  __shared__ int s_max[8];
+  const int tid = threadIdx.x;
+  constexpr int ITEMS = 16;
+  while (true) {
+    if (tid == 0) s_misc[0] = atomicAdd(queue, 1u);
+    __syncthreads();
+    const int t = (int)s_misc[0];
+    if (t >= B.T4) return;
+    const int4 d = B.tiles4k[t];
+    const int c = d.z, cs = B.start[c];
+    const int n = max(unique_c[c] - 1, 0);  // radix nodes of this cloud
+    const int lo = d.x - cs;                // first node of the tile (cloud-local)
+    if (lo >= n) {                          // past this cloud's nodes: nobody waits on it
+      __syncthreads();
+      continue;
+    }
+    const uint8_t* pn = prefix_n + cs;
+    const int* par = parent + cs;
+    const int j0 = lo + tid * ITEMS;
+    int v[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const int i = j0 + k;
+      int e = 0;
+      if (i > 0 && i < n) {
+        int p = par[i];
+        if ((unsigned)p >= (unsigned)n) {
+          raise_status(status, kStatusWalkLimit);
+          p = 0;
+        }
+        e = (int)(pn[i] / 3) - (int)(pn[p] / 3);
+      }
+      v[k] = e;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) sum += (uint32_t)v[k];
+    const uint32_t off = block_exclusive_sum<256>(sum, s_warp, &s_misc[2]);
+    if (tid < 32) {
+      const uint32_t e = chain_lookback(lb, t, d.w, s_misc[2], status);
+      if (tid == 0) s_misc[3] = e;
+    }
+    __syncthreads();
+    uint32_t run = s_misc[3] + off;
+    int mx = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const int i = j0 + k;
+      run += (uint32_t)v[k];
+      if (i < n) {
+        ec_out[cs + i] = v[k];
+        ps_out[cs + i] = (int)run;
+        const int last = v[k] > 0 ? (int)run + v[k] - 1 : (int)run;
+        if (i > 0 && v[k] > 0 && last > mx) mx = last;
+        if (i == n - 1 && (int)run > mx) mx = (int)run;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) s_max[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+      int m = 0;
+      for (int w = 0; w < 8; ++w) m = max(m, s_max[w]);
+      atomicMax(&max_slot_c[c], m);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ octree --
+struct BatchOctDev {
+  oct_node* nodes;
+  const int* offsets;
+  const int* counts;
+  const uint32_t* codes;
+  const uint8_t* prefix_n;
+  const uint8_t* hll;
+  const uint8_t* hlr;
+  const int* parent;
+  const int* left_child;
+  const int* unique_c;
+  const int* max_slot_c;
+  OctTags tags;  // over the whole node capacity
+};
+
+struct CloudSizes {
+  int c, n_brt, n_oct, cap, ns;
+  bool fits;
+};
+
+__device__ __forceinline__ CloudSizes cloud_sizes(const BatchDev& B, const BatchOctDev& O, int c) {
+  CloudSizes z;
+  z.c = c;
+  z.n_brt = max(O.unique_c[c] - 1, 0);
+  z.n_oct = z.n_brt >= 1 ? O.max_slot_c[c] + 1 : 0;
+  z.ns = B.node_start[c];
+  z.cap = B.node_start[c + 1] - z.ns;
+  z.fits = z.n_oct <= z.cap;
+  return z;
+}
+
+__device__ __forceinline__ OctArgs cloud_view(const BatchDev& B, const BatchOctDev& O,
+                                              const CloudSizes& z) {
+  const int cs = B.start[z.c];
+  OctArgs a{};
+  a.nodes = O.nodes + z.ns;
+  a.cap = z.cap;
+  a.offsets = O.offsets + cs;
+  a.counts = O.counts + cs;
+  a.codes = O.codes + cs;
+  a.prefix_n = O.prefix_n + cs;
+  a.hll = O.hll + cs;
+  a.hlr = O.hlr + cs;
+  a.parent = O.parent + cs;
+  a.left_child = O.left_child + cs;
+  a.min_coord = B.mins[z.c];
+  a.range = B.ranges[z.c];
+  a.n_brt_host = z.n_brt;
+  a.n_oct_host = z.n_oct;
+  return a;
+}
+
+__device__ __forceinline__ OctTags cloud_tags(const BatchOctDev& O, const CloudSizes& z) {
+  OctTags t;
+  t.child = O.tags.child + (size_t)z.ns * 8;
+  t.owner = O.tags.owner + z.ns;
+  t.mask = O.tags.mask + z.ns;
+  t.cap = z.cap;
+  return t;
+}
+
+__global__ void __launch_bounds__(256)
+    batch_oct_zero_kernel(BatchDev B, BatchOctDev O, int total_cap, uint32_t* __restrict__ status) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total_cap; g += gridDim.x * blockDim.x) {
+    const int c = cloud_of(B.node_start, B.C, g);
+    const CloudSizes z = cloud_sizes(B, O, c);
+    const int p = g - z.ns;
+    if (!z.fits) {
+      if (p == 0) raise_status(status, kStatusCapacity);
+      continue;
+    }
+    if (p < z.n_oct) {
+      uint4* c4 = reinterpret_cast<uint4*>(O.tags.child);
+      c4[2 * (size_t)g] = make_uint4(0, 0, 0, 0);
+      c4[2 * (size_t)g + 1] = make_uint4(0, 0, 0, 0);
+      O.tags.owner[g] = 0;
+      O.tags.mask[g] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    batch_oct_emit_kernel(BatchDev B, BatchOctDev O, uint32_t* __restrict__ status) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < B.N; g += gridDim.x * blockDim.x) {
+    const int c = cloud_of(B.start, B.C, g);
+    const CloudSizes z = cloud_sizes(B, O, c);
+    const int i = g - B.start[c];
+    if (i >= z.n_brt || !z.fits) continue;
+    const OctArgs a = cloud_view(B, O, z);
+    Sizes zz;
+    zz.n_brt = z.n_brt;
+    zz.n_oct = z.n_oct;
+    zz.fits = true;
+    emit_node(kOctMake | kOctLink, i, a, cloud_tags(O, z), zz, status);
+  }
+}
+
+__global__ void __launch_bounds__(kFinThreads)
+    batch_oct_finalize_kernel(BatchDev B, BatchOctDev O, int total_cap) {
+  __shared__ int s_nodes[kFinThreads * kNodeWords];
+  __shared__ uint8_t s_valid[kFinThreads];
+  int* out_words = reinterpret_cast<int*>(O.nodes);
+  for (int blk = blockIdx.x * kFinThreads; blk < total_cap; blk += gridDim.x * kFinThreads) {
+    const int g = blk + threadIdx.x;
+    bool valid = false;
+    if (g < total_cap) {
+      const int c = cloud_of(B.node_start, B.C, g);
+      const CloudSizes z = cloud_sizes(B, O, c);
+      const int p = g - z.ns;
+      valid = z.fits && z.n_brt >= 1 && p < z.n_oct;
+      if (valid) {
+        const OctArgs a = cloud_view(B, O, z);
+        finalize_slot(true, p, a, cloud_tags(O, z), a.prefix_n[0] / 3,
+                      s_nodes + threadIdx.x * kNodeWords);
+      }
+    }
+    s_valid[threadIdx.x] = valid;
+    __syncthreads();
+    const int count = min(kFinThreads, total_cap - blk);
+    int* dst = out_words + (size_t)blk * kNodeWords;
+    for (int k = threadIdx.x; k < count * kNodeWords; k += kFinThreads)
+      if (s_valid[k / kNodeWords]) dst[k] = s_nodes[k];
+    __syncthreads();
+  }
+}
+
+__global__ void batch_publish_kernel(BatchDev B, BatchOctDev O, const uint32_t* status,
+                                     int* __restrict__ counts) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < B.C; c += gridDim.x * blockDim.x) {
+    const CloudSizes z = cloud_sizes(B, O, c);
+    counts[4 * c + 0] = O.unique_c[c];
+    counts[4 * c + 1] = z.n_brt;
+    counts[4 * c + 2] = z.n_oct;
+    counts[4 * c + 3] = (int)((z.fits ? 0u : kStatusCapacity) | (*status & ~kStatusCapacity));
+  }
+}
+
+}  // namespace octgb
+
+// ----------------------------------------------------------------- plan + ABI --
+struct oct_batch_plan {
+  int C = 0;
+  int N = 0;
+  int total_cap = 0;
+  octgb::SortPlan sp{};
+  std::vector<int> start, node_start, cloud_tile0;
+  std::vector<int4> sort_tiles, tiles4k;
+  // device tables (caller buffer) offsets
+  size_t t_start = 0, t_node_start = 0, t_tile0 = 0, t_sort = 0, t_4k = 0, tables_bytes = 0;
+  // workspace offsets
+  size_t w_status = 0, w_unique = 0, w_maxslot = 0, w_hist = 0, w_queues = 0, w_lb_u = 0,
+         w_lb_s = 0, zero_bytes = 0, w_base = 0, w_th = 0, w_keys_a = 0, w_keys_b = 0,
+         w_tags = 0, ws_bytes = 0;
+};
+
+namespace {
+
+using octgb::align_up;
+
+int batch_fail(cudaError_t e, const char* where) {
+  char msg[192];
+  snprintf(msg, sizeof(msg), "%s: %s", where, cudaGetErrorString(e));
+  octgb::set_last_error(msg);
+  return OCT_ERR_CUDA;
+}
+
+octgb::BatchDev dev_view(const oct_batch_plan* P, const void* tables, const float* mins,
+                         const float* ranges) {
+  const char* t = static_cast<const char*>(tables);
+  octgb::BatchDev B;
+  B.C = P->C;
+  B.N = P->N;
+  B.start = reinterpret_cast<const int*>(t + P->t_start);
+  B.node_start = reinterpret_cast<const int*>(t + P->t_node_start);
+  B.mins = mins;
+  B.ranges = ranges;
+  B.sort_tiles = reinterpret_cast<const int4*>(t + P->t_sort);
+  B.Ts = (int)P->sort_tiles.size();
+  B.cloud_tile0 = reinterpret_cast<const int*>(t + P->t_tile0);
+  B.tiles4k = reinterpret_cast<const int4*>(t + P->t_4k);
+  B.T4 = (int)P->tiles4k.size();
+  return B;
+}
+
+}  // namespace
+
+extern "C" {
+
+OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_sizes,
+                                              const int32_t* h_node_caps) {
+  using namespace octgb;
+  if (n_clouds < 1 || !h_sizes) return nullptr;
+  oct_batch_plan* P = new (std::nothrow) oct_batch_plan();
+  if (!P) return nullptr;
+  P->C = n_clouds;
+  long long N = 0, cap = 0;
+  P->start.resize(n_clouds + 1);
+  P->node_start.resize(n_clouds + 1);
+  for (int c = 0; c < n_clouds; ++c) {
+    if (h_sizes[c] < 0 || (h_node_caps && h_node_caps[c] < 0)) {
+      delete P;
+      return nullptr;
+    }
+    P->start[c] = (int)N;
+    P->node_start[c] = (int)cap;
+    N += h_sizes[c];
+    cap += h_node_caps ? h_node_caps[c] : h_sizes[c];
+    if (N > OCT_MAX_N || cap > OCT_MAX_N) {
+      delete P;
+      return nullptr;
+    }
+  }
+  P->start[n_clouds] = (int)N;
+  P->node_start[n_clouds] = (int)cap;
+  P->N = (int)N;
+  P->total_cap = (int)cap;
+  SortConfig cfg = get_sort_config();
+  cfg.scan = 1;  // batched passes use per-cloud tile prefixes
+  P->sp = sort_plan_cfg(P->N, 30, cfg);
+  const int tile = P->sp.tile;
+  P->cloud_tile0.resize(n_clouds + 1);
+  for (int c = 0; c < n_clouds; ++c) {
+    P->cloud_tile0[c] = (int)P->sort_tiles.size();
+    const int f4 = (int)P->tiles4k.size();
+    for (int lo = P->start[c]; lo < P->start[c + 1]; lo += tile)
+      P->sort_tiles.push_back(make_int4(lo, std::min(lo + tile, P->start[c + 1]), c, P->cloud_tile0[c]));
+    for (int lo = P->start[c]; lo < P->start[c + 1]; lo += kBatchTile4k)
+      P->tiles4k.push_back(make_int4(lo, std::min(lo + kBatchTile4k, P->start[c + 1]), c, f4));
+  }
+  P->cloud_tile0[n_clouds] = (int)P->sort_tiles.size();
+  size_t o = 0;
+  auto take = [&](size_t b) {
+    const size_t at = o;
+    o = align_up(o + b, 256);
+    return at;
+  };
+  P->t_start = take(4 * (size_t)(n_clouds + 1));
+  P->t_node_start = take(4 * (size_t)(n_clouds + 1));
+  P->t_tile0 = take(4 * (size_t)(n_clouds + 1));
+  P->t_sort = take(16 * (P->sort_tiles.size() + 1));
+  P->t_4k = take(16 * (P->tiles4k.size() + 1));
+  P->tables_bytes = o;
+  const int passes = P->sp.passes, bins = P->sp.bins;
+  o = 0;
+  P->w_status = take(4);
+  P->w_unique = take(4 * (size_t)n_clouds);
+  P->w_maxslot = take(4 * (size_t)n_clouds);
+  P->w_hist = take(4 * (size_t)n_clouds * passes * bins);
+  P->w_queues = take(64);
+  P->w_lb_u = take(8 * (P->tiles4k.size() + 1));
+  P->w_lb_s = take(8 * (P->tiles4k.size() + 1));
+  P->zero_bytes = o;
+  P->w_base = take(4 * (size_t)n_clouds * passes * bins);
+  P->w_th = take(4 * (P->sort_tiles.size() + 1) * bins);
+  P->w_keys_a = take(4 * (size_t)std::max(P->N, 1));
+  P->w_keys_b = take(4 * (size_t)std::max(P->N, 1));
+  P->w_tags = take(oct_tags_bytes(std::max(P->total_cap, 1)));
+  P->ws_bytes = o;
+  return P;
+}
+
+OCT_API void oct_batch_plan_destroy(oct_batch_plan* P) { delete P; }
+
+OCT_API int oct_batch_plan_info(const oct_batch_plan* P, int64_t out[6]) {
+  if (!P || !out) return OCT_ERR_INVALID_ARG;
+  out[0] = P->C;
+  out[1] = P->N;
+  out[2] = P->total_cap;
+  out[3] = (int64_t)P->tables_bytes;
+  out[4] = (int64_t)P->ws_bytes;
+  out[5] = (int64_t)P->sort_tiles.size();
+  return OCT_OK;
+}
+
+OCT_API int oct_batch_upload_tables(const oct_batch_plan* P, void* d_tables, oct_stream_t stream) {
+  if (!P || !d_tables || (reinterpret_cast<uintptr_t>(d_tables) & 255)) return OCT_ERR_INVALID_ARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char* t = static_cast<char*>(d_tables);
+  cudaError_t e = cudaMemcpyAsync(t + P->t_start, P->start.data(), 4 * P->start.size(),
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(t + P->t_node_start, P->node_start.data(), 4 * P->node_start.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(t + P->t_tile0, P->cloud_tile0.data(), 4 * P->cloud_tile0.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !P->sort_tiles.empty())
+    e = cudaMemcpyAsync(t + P->t_sort, P->sort_tiles.data(), 16 * P->sort_tiles.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !P->tiles4k.empty())
+    e = cudaMemcpyAsync(t + P->t_4k, P->tiles4k.data(), 16 * P->tiles4k.size(),
+                        cudaMemcpyHostToDevice, s);
+  // the host vectors live in the plan: wait so the copies have read them
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? OCT_OK : batch_fail(e, "oct_batch_upload_tables");
+}
+
+OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables,
+                                   const oct_vec4* points, const float* d_mins,
+                                   const float* d_ranges, const oct_build_outputs* out,
+                                   int32_t* d_cloud_counts, void* workspace,
+                                   size_t workspace_bytes, oct_stream_t stream) {
+  using namespace octgb;
+  if (!P || !d_tables || !d_mins || !d_ranges || !out || !d_cloud_counts || !workspace ||
+      (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return OCT_ERR_INVALID_ARG;
+  if (workspace_bytes < P->ws_bytes) return OCT_ERR_WORKSPACE;
+  if (P->N > 0 && (!points || (reinterpret_cast<uintptr_t>(points) & 15) || !out->codes ||
+                   !out->tree.prefix_n || !out->tree.has_leaf_left || !out->tree.has_leaf_right ||
+                   !out->tree.left_child || !out->tree.parent || !out->edge_count ||
+                   !out->prefix_sum || !out->nodes || out->nodes_capacity < P->total_cap))
+    return OCT_ERR_INVALID_ARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char* w = static_cast<char*>(workspace);
+  const BatchDev B = dev_view(P, d_tables, d_mins, d_ranges);
+  uint32_t* status = reinterpret_cast<uint32_t*>(w + P->w_status);
+  int* unique_c = reinterpret_cast<int*>(w + P->w_unique);
+  int* max_slot_c = reinterpret_cast<int*>(w + P->w_maxslot);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(w + P->w_hist);
+  uint32_t* queues = reinterpret_cast<uint32_t*>(w + P->w_queues);
+  unsigned long long* lb_u = reinterpret_cast<unsigned long long*>(w + P->w_lb_u);
+  unsigned long long* lb_s = reinterpret_cast<unsigned long long*>(w + P->w_lb_s);
+  uint32_t* base = reinterpret_cast<uint32_t*>(w + P->w_base);
+  uint32_t* th = reinterpret_cast<uint32_t*>(w + P->w_th);
+  uint32_t* ka = reinterpret_cast<uint32_t*>(w + P->w_keys_a);
+  uint32_t* kb = reinterpret_cast<uint32_t*>(w + P->w_keys_b);
+  const SortPlan& sp = P->sp;
+  const int passes = sp.passes, bins = sp.bins, rb = sp.radix_bits;
+  const int sms = device_sm_count();
+  cudaError_t e = cudaMemsetAsync(w, 0, P->zero_bytes, s);
+  if (e != cudaSuccess) return batch_fail(e, "batch: clear");
+  if (P->N > 0) {
+    const int mgrid = std::max(1, std::min(B.Ts, sms * 4));
+    const size_t msm = 4 * (size_t)passes * bins;
+    if (rb == 10) {
+      batch_morton_kernel<10><<<mgrid, 256, msm, s>>>(reinterpret_cast<const float4*>(points), ka,
+                                                      B, hist, passes, status);
+      batch_hist_scan_kernel<10><<<P->C * passes, 1024, 0, s>>>(hist, base, B, passes);
+    } else {
+      batch_morton_kernel<8><<<mgrid, 256, msm, s>>>(reinterpret_cast<const float4*>(points), ka,
+                                                     B, hist, passes, status);
+      batch_hist_scan_kernel<8><<<P->C * passes, 256, 0, s>>>(hist, base, B, passes);
+    }
+    uint32_t* a = ka;
+    uint32_t* b = kb;
+    for (int p = 0; p < passes && e == cudaSuccess; ++p) {
+      const int shift = p * rb;
+      e = launch_tile_hist(rb, a, P->N, shift, B.sort_tiles, B.Ts, th, s);
+      if (e != cudaSuccess) break;
+      batch_tile_scan_kernel<<<dim3(P->C, (bins + 31) / 32), 1024, 0, s>>>(th, bins, base, passes,
+                                                                           p, B);
+      e = launch_pass(sp, p > 0, a, b, shift, nullptr, nullptr, nullptr, th, status, nullptr, s,
+                      B.sort_tiles, B.Ts);
+      uint32_t* t = a;
+      a = b;
+      b = t;
+    }
+    if (e != cudaSuccess) return batch_fail(e, "batch: sort");
+    const int qgrid = std::max(1, std::min(B.T4, sms * 8));
+    batch_unique_kernel<<<qgrid, kBuThreads, 0, s>>>(a, out->codes, B, unique_c, lb_u, queues,
+                                                     status);
+    const int ngrid = std::max(1, std::min((P->N + 255) / 256, sms * 16));
+    batch_tree_kernel<<<ngrid, 256, 0, s>>>(out->codes, B, unique_c, out->tree.prefix_n,
+                                            out->tree.has_leaf_left, out->tree.has_leaf_right,
+                                            out->tree.left_child, out->tree.parent);
+    batch_edge_scan_kernel<<<qgrid, 256, 0, s>>>(B, unique_c, out->tree.prefix_n, out->tree.parent,
+                                                 out->edge_count, out->prefix_sum, max_slot_c,
+                                                 lb_s, queues + 1, status);
+    BatchOctDev O;
+    O.nodes = out->nodes;
+    O.offsets = out->prefix_sum;
+    O.counts = out->edge_count;
+    O.codes = out->codes;
+    O.prefix_n = out->tree.prefix_n;
+    O.hll = out->tree.has_leaf_left;
+    O.hlr = out->tree.has_leaf_right;
+    O.parent = out->tree.parent;
+    O.left_child = out->tree.left_child;
+    O.unique_c = unique_c;
+    O.max_slot_c = max_slot_c;
+    O.tags = oct_tags_carve(w + P->w_tags, std::max(P->total_cap, 1));
+    const int cgrid = std::max(1, std::min((P->total_cap + 255) / 256, sms * 16));
+    batch_oct_zero_kernel<<<cgrid, 256, 0, s>>>(B, O, P->total_cap, status);
+    batch_oct_emit_kernel<<<ngrid, 256, 0, s>>>(B, O, status);
+    batch_oct_finalize_kernel<<<cgrid, kFinThreads, 0, s>>>(B, O, P->total_cap);
+    batch_publish_kernel<<<(P->C + 255) / 256, 256, 0, s>>>(B, O, status, d_cloud_counts);
+  } else {
+    e = cudaMemsetAsync(d_cloud_counts, 0, 16 * (size_t)P->C, s);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? OCT_OK : batch_fail(e, "oct_build_octree_batch");
+}
+
+}  // extern "C"

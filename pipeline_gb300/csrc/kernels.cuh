@@ -11,7 +11,7 @@
 
 namespace octgb {
 
-static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+__host__ __device__ static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Optional per-launch event recording (timed builds): mark() records the next
 // caller event on the stream after a launch.
@@ -35,6 +35,14 @@ int device_sm_count();
 void set_last_error(const char* msg);
 
 // ---- sort ----------------------------------------------------------------
+// Tunable shape of the radix sort (chosen by the autotuner or the default).
+struct SortConfig {
+  int radix_bits;  // 10 (3 passes over 30-bit keys) or 8
+  int warps;       // warps per tile CTA (16)
+  int items;       // keys per thread (16 or 24)
+  int scan;        // 0: decoupled look-back (OneSweep); 1: tile histograms + tile scan
+};
+
 struct SortPlan {
   int n;
   int radix_bits;
@@ -42,11 +50,24 @@ struct SortPlan {
   int bins;
   int tile;
   int tiles;
-  size_t hist_off, base_off, counter_off, lookback_off;
-  size_t bytes;  // control block, zeroed before each sort
+  SortConfig cfg;
+  size_t hist_off, counter_off, lookback_off, base_off, tile_hist_off;
+  size_t zero_bytes;  // [0, zero_bytes) is cleared before each sort
+  size_t bytes;       // whole control block
 };
 
 SortPlan sort_plan(int n, int key_bits);
+SortPlan sort_plan_cfg(int n, int key_bits, SortConfig cfg);
+// One digit pass (batched sorts: tile descriptors int4{first, end, cloud,
+// first tile of cloud} and their count; nullptr / 0 for a single array).
+cudaError_t launch_pass(const SortPlan& p, bool stable, const uint32_t* src, uint32_t* dst,
+                        int shift, const uint32_t* base, uint32_t* lookback, uint32_t* counter,
+                        const uint32_t* tile_prefix, uint32_t* status, const uint32_t* gate,
+                        cudaStream_t s, const int4* tdesc, int tiles);
+cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
+                             const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s);
+void set_sort_config(const SortConfig& c);
+SortConfig get_sort_config();
 
 // Morton encode; with plan != nullptr also accumulates the plan's digit
 // histograms into the zeroed control block ctrl.
@@ -58,6 +79,12 @@ cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* c
 cudaError_t launch_sort_passes(uint32_t* keys, uint32_t* alt, const SortPlan* plan, void* ctrl,
                                uint32_t* status, cudaStream_t s, uint32_t** result,
                                Recorder* rec = nullptr);
+// Gated forms: the kernels return at once unless *gate != 0 (device flag).
+cudaError_t launch_histogram_gated(const uint32_t* keys, const SortPlan* plan, void* ctrl,
+                                   const uint32_t* gate, cudaStream_t s);
+cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
+                                     void* ctrl, uint32_t* status, const uint32_t* gate,
+                                     cudaStream_t s, uint32_t** result);
 
 // ---- unique --------------------------------------------------------------
 struct ScanPlan {
@@ -72,6 +99,9 @@ ScanPlan unique_plan(int n);
 // writes U to *d_count.
 cudaError_t launch_unique(const uint32_t* src, uint32_t* dst, int n, int* d_count,
                           const ScanPlan* plan, void* ctrl, uint32_t* status, cudaStream_t s);
+cudaError_t launch_unique_gated(const uint32_t* src, uint32_t* dst, int n, int* d_count,
+                                const ScanPlan* plan, void* ctrl, uint32_t* status,
+                                const uint32_t* gate, cudaStream_t s);
 
 // ---- radix tree, edge count, prefix sum -----------------------------------
 // n_nodes from the host (n_host) or, when d_unique != nullptr, as *d_unique - 1.

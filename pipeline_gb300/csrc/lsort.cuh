@@ -1,0 +1,40 @@
+// Learned bucketed sort + unique: plan and launch interface.
+#pragma once
+
+#include "learned.cuh"
+
+namespace octgb {
+
+// Device-side statistics of one learned sort (in the zeroed workspace).
+struct LsortStats {
+  uint32_t fallback;        // 1: the OneSweep path produced the result
+  uint32_t failed_buckets;  // buckets that fit neither bucket form
+  uint32_t overflow_keys;   // keys in buckets above the bitonic capacity
+  uint32_t max_bucket;      // largest bucket
+  uint32_t n;
+  float overflow_frac;      // overflow_keys / n
+  uint32_t skip;            // set before the scatter when overflow_frac > threshold
+  uint32_t pad;
+};
+
+struct LsortPlan {
+  int n, nb, chunks;
+  LcdfLayout L;
+  SortPlan fallback_sort;
+  ScanPlan fallback_unique;
+  size_t stats_off, counter_off, lookback_off, sort_ctrl_off, uniq_ctrl_off, zero_bytes;
+  size_t hist_off, totals_off, starts_off, bkeys_off, alt_off, bytes;
+};
+
+LsortPlan lsort_plan(int n, int nb, int max_segments);
+size_t lsort_hist_smem(int nb, int max_segments);
+constexpr int kLsortMaxSmem = 227 * 1024;  // dynamic shared memory per CTA on sm_103
+
+// Sorted unique keys into `out`, U into *d_unique. With pts != nullptr the
+// keys are Morton-encoded from the points first (into `keys`).
+cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coord, float range,
+                         const char* blob, const LsortPlan& p, char* ws, float threshold,
+                         uint32_t* out, int* d_unique, uint32_t* status, cudaStream_t s,
+                         Recorder* rec);
+
+}  // namespace octgb

@@ -23,11 +23,9 @@
 // Sequence tags (32-bit, larger = later):
 //   MakeOctNodes step j of node i : ((i << 4) | j) + 1        (i < 2^27)
 //   LinkLeafNodes side s of node i: 0x80000000 | (i << 1) | s
-#include "kernels.cuh"
+#include "octree.cuh"
 
 namespace octgb {
-
-constexpr uint32_t kLinkTag = 0x80000000u;
 
 size_t oct_tags_bytes(int cap) {
   const size_t c = cap > 0 ? (size_t)cap : 1;
@@ -47,22 +45,6 @@ OctTags oct_tags_carve(void* base, int cap) {
   return t;
 }
 
-struct Sizes {
-  int n_brt, n_oct;
-  bool fits;
-};
-
-__device__ __forceinline__ Sizes read_sizes(const OctArgs& a) {
-  Sizes z;
-  z.n_brt = a.d_unique ? max(*a.d_unique - 1, 0) : a.n_brt_host;
-  if (a.d_max_slot)
-    z.n_oct = z.n_brt >= 1 ? *a.d_max_slot + 1 : 0;
-  else
-    z.n_oct = a.n_oct_host;
-  z.fits = z.n_oct <= a.cap;
-  return z;
-}
-
 __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
                                                        uint32_t* __restrict__ status) {
   const Sizes z = read_sizes(a);
@@ -80,96 +62,14 @@ __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
   }
 }
 
-__device__ __forceinline__ void put_child(const OctTags& t, int slot, int which, uint32_t tag,
-                                          int n_oct, uint32_t* status) {
-  if ((unsigned)slot >= (unsigned)n_oct) {
-    raise_status(status, kStatusCapacity);
-    return;
-  }
-  atomicMax(&t.child[(size_t)slot * 8 + which], tag);
-}
-
 __global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctTags t,
                                                        uint32_t* __restrict__ status) {
   const Sizes z = read_sizes(a);
   if (!z.fits) return;
   const int stride = gridDim.x * blockDim.x;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < z.n_brt; i += stride) {
-    const int L = a.prefix_n[i] / 3;
-    if ((mode & kOctMake) && i >= 1) {
-      // include/shared/oct.h:24-90
-      const int k = a.counts[i];
-      if (k > 0) {
-        const int base = a.offsets[i];
-        const uint32_t code = a.codes[i];
-        for (int j = 0; j < k - 1; ++j) {
-          const int level = L - j;
-          const uint32_t pre = code >> (30 - 3 * level);
-          const int which = (int)(pre & 7u);
-          const int up = base + j + 1;
-          put_child(t, up, which, (((uint32_t)i << 4) | (uint32_t)j) + 1u, z.n_oct, status);
-          if ((unsigned)up < (unsigned)z.n_oct) atomicOr(&t.mask[up], 1u << which);
-          if ((unsigned)(base + j) < (unsigned)z.n_oct) atomicMax(&t.owner[base + j], (uint32_t)i);
-        }
-        int rp = a.parent[i];
-        int counter = 0;
-        bool bad = (unsigned)rp >= (unsigned)z.n_brt;
-        while (!bad && a.counts[rp] == 0) {
-          rp = a.parent[rp];
-          bad = (unsigned)rp >= (unsigned)z.n_brt;
-          if (++counter > 30) break;
-        }
-        if (bad) {  // malformed parent[]: never read out of bounds
-          raise_status(status, kStatusWalkLimit);
-          rp = 0;
-        }
-        const int top = L - k + 1;
-        const int which = (int)((code >> (30 - 3 * top)) & 7u);
-        const int oct_parent = a.offsets[rp];
-        put_child(t, oct_parent, which, (((uint32_t)i << 4) | (uint32_t)(k - 1)) + 1u, z.n_oct,
-                  status);
-        if ((unsigned)oct_parent < (unsigned)z.n_oct) atomicOr(&t.mask[oct_parent], 1u << which);
-        const int slot = base + k - 1;
-        if ((unsigned)slot < (unsigned)z.n_oct) atomicMax(&t.owner[slot], (uint32_t)i);
-        else raise_status(status, kStatusCapacity);
-      }
-    }
-    if (mode & kOctLink) {
-      // include/shared/oct.h:92-134, walk bounded at radix node 0.
-      const bool l = a.hll[i], r = a.hlr[i];
-      if (l || r) {
-        int rn = i, steps = 0;
-        while (a.counts[rn] == 0 && rn != 0) {
-          const int up = a.parent[rn];
-          if ((unsigned)up >= (unsigned)z.n_brt || ++steps > 64) {
-            raise_status(status, kStatusWalkLimit);
-            break;
-          }
-          rn = up;
-        }
-        const int dst = a.offsets[rn];
-        const uint32_t sh = (uint32_t)(30 - 3 * (L + 1)) & 31u;
-        int lc = a.left_child[i];
-        if ((unsigned)lc >= (unsigned)z.n_brt) {  // leaf index lc + 1 <= n_brt must hold
-          raise_status(status, kStatusWalkLimit);
-          continue;
-        }
-        if (l)
-          put_child(t, dst, (int)((a.codes[lc] >> sh) & 7u), kLinkTag | ((uint32_t)i << 1),
-                    z.n_oct, status);
-        if (r)
-          put_child(t, dst, (int)((a.codes[lc + 1] >> sh) & 7u),
-                    kLinkTag | ((uint32_t)i << 1) | 1u, z.n_oct, status);
-      }
-    }
-  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < z.n_brt; i += stride)
+    emit_node(mode, i, a, t, z, status);
 }
-
-// One thread per slot computes the node; the block stages its 256 nodes
-// (15 KB) in shared memory and writes them as consecutive 32-bit words, so
-// every warp store is one contiguous 128-byte line.
-constexpr int kFinThreads = 256;
-constexpr int kNodeWords = 15;
 
 __global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
   __shared__ int s_nodes[kFinThreads * kNodeWords];
@@ -177,68 +77,11 @@ __global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, Oct
   if (!z.fits || z.n_brt < 1) return;
   const int root_level = a.prefix_n[0] / 3;
   const bool fresh = mode & kOctFresh;
-  const uint4* c4 = reinterpret_cast<const uint4*>(t.child);
   int* out_words = reinterpret_cast<int*>(a.nodes);
   for (int blk = blockIdx.x * kFinThreads; blk < z.n_oct; blk += gridDim.x * kFinThreads) {
     const int p = blk + threadIdx.x;
     const int count = min(kFinThreads, z.n_oct - blk);
-    if (p < z.n_oct) {
-      const uint4 ta = c4[2 * p], tb = c4[2 * p + 1];
-      const uint32_t tags[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
-      const oct_node* nd = a.nodes + p;
-      int* w = s_nodes + threadIdx.x * kNodeWords;
-      uint32_t link_bits = 0;
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const uint32_t g = tags[c];
-        int v;
-        if (g == 0) {
-          v = fresh ? 0 : nd->children[c];
-        } else if (g & kLinkTag) {
-          const int i = (int)((g & ~kLinkTag) >> 1);
-          v = a.left_child[i] + (int)(g & 1u);
-          link_bits |= 1u << c;
-        } else {
-          const uint32_t q = g - 1u;
-          v = a.offsets[q >> 4] + (int)(q & 15u);
-        }
-        w[c] = v;
-      }
-      const uint32_t m = t.mask[p];
-      const uint32_t own = t.owner[p];
-      float4 corner;
-      float cell;
-      if (own != 0) {
-        const int i = (int)own;
-        const int j = p - a.offsets[i];
-        const int level = a.prefix_n[i] / 3 - j;
-        const int sh = 30 - 3 * level;
-        corner = decode_corner((a.codes[i] >> sh) << sh, a.min_coord, a.range);
-        cell = __fdiv_rn(a.range, (float)(1 << (level - root_level)));
-      } else if (fresh && p == 0) {
-        const int sh = 30 - 3 * root_level;
-        corner = decode_corner((a.codes[0] >> sh) << sh, a.min_coord, a.range);
-        cell = a.range;
-      } else if (fresh) {
-        corner = make_float4(0.f, 0.f, 0.f, 0.f);
-        cell = 0.f;
-      } else {
-        corner = make_float4(nd->corner.x, nd->corner.y, nd->corner.z, nd->corner.w);
-        cell = nd->cell_size;
-      }
-      w[8] = __float_as_int(corner.x);
-      w[9] = __float_as_int(corner.y);
-      w[10] = __float_as_int(corner.z);
-      w[11] = __float_as_int(corner.w);
-      w[12] = __float_as_int(cell);
-      if (fresh) {
-        w[13] = (int)m;
-        w[14] = 0;
-      } else {
-        w[13] = nd->child_node_mask | (int)m;
-        w[14] = nd->child_leaf_mask & ~(int)link_bits;
-      }
-    }
+    if (p < z.n_oct) finalize_slot(fresh, p, a, t, root_level, s_nodes + threadIdx.x * kNodeWords);
     __syncthreads();
     int* dst = out_words + (size_t)blk * kNodeWords;
     for (int k = threadIdx.x; k < count * kNodeWords; k += kFinThreads) dst[k] = s_nodes[k];

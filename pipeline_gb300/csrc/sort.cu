@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(256)
 template <int RB>
 __global__ void __launch_bounds__(256)
     histogram_kernel(const uint32_t* __restrict__ keys, int n, uint32_t* __restrict__ ghist,
-                     int passes) {
+                     int passes, const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   constexpr int BINS = 1 << RB;
   extern __shared__ uint32_t s_hist[];
   for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x) s_hist[i] = 0;
@@ -103,7 +104,9 @@ __global__ void __launch_bounds__(256)
 // Exclusive scan of each pass's histogram: one block of BINS/… threads per pass.
 template <int RB>
 __global__ void __launch_bounds__(1024) hist_scan_kernel(const uint32_t* __restrict__ ghist,
-                                                         uint32_t* __restrict__ base) {
+                                                         uint32_t* __restrict__ base,
+                                                         const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   constexpr int BINS = 1 << RB;
   constexpr int T = BINS < 1024 ? BINS : 1024;
   constexpr int PER = BINS / T;
@@ -127,7 +130,21 @@ __global__ void __launch_bounds__(1024) hist_scan_kernel(const uint32_t* __restr
 }
 
 // --------------------------------------------------------------------------
-// One OneSweep digit pass.
+// One LSD digit pass over tiles of WARPS*32*ITEMS keys.
+//
+// Ranking (position of a key among the tile's keys with its digit):
+//   STABLE  warp multi-split from RB ballots (peers = lanes with the same
+//           digit), counted per warp in shared memory, then offset across
+//           warps: stable in (warp, item, lane) order, which is input order.
+//   !STABLE one shared-memory atomicAdd per key: any order. Only the first
+//           LSD pass may use it (its input order carries no information).
+// Tile offsets (where the tile's keys of each digit start in the output):
+//   SCAN 0  decoupled look-back over earlier tiles (OneSweep): a tile takes
+//           the next id from an atomic counter, publishes its per-digit
+//           counts, sums earlier tiles' counts back to an inclusive prefix
+//           (bounded waits, windowed relaxed loads).
+//   SCAN 1  precomputed: a per-tile digit histogram kernel and a tile-prefix
+//           scan ran before the pass (reduce-then-scan); no inter-tile waits.
 //   lookback[tile * BINS + b]: bits 31..30 flag (0 not ready, 1 tile count,
 //   2 inclusive count of tiles 0..tile), bits 29..0 the count.
 // --------------------------------------------------------------------------
@@ -136,39 +153,57 @@ constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kFlagMask = 3u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 
-template <int RB, int WARPS, int ITEMS>
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int RB, int WARPS, int ITEMS, bool STABLE>
 struct PassSmem {
   static constexpr int BINS = 1 << RB;
   static constexpr int TILE = WARPS * 32 * ITEMS;
-  static constexpr int HIST_BYTES = WARPS * BINS * 2;
+  static constexpr int HIST_BYTES = STABLE ? WARPS * BINS * 2 : BINS * 4;
   static constexpr int STAGE_BYTES = TILE * 4;
-  static constexpr int UNION_BYTES = HIST_BYTES > STAGE_BYTES ? HIST_BYTES : STAGE_BYTES;
+  // the stable per-warp counters are dead once positions are known: alias them
+  static constexpr int UNION_BYTES =
+      STABLE ? (HIST_BYTES > STAGE_BYTES ? HIST_BYTES : STAGE_BYTES) : HIST_BYTES + STAGE_BYTES;
   static constexpr int BYTES = UNION_BYTES + BINS * 4 * 2 + 64 * 4;
 };
 
-template <int RB, int WARPS, int ITEMS>
-__global__ void __launch_bounds__(WARPS * 32, 2)
-    onesweep_pass_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int n,
-                         int shift, const uint32_t* __restrict__ bin_base,
-                         uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter,
-                         uint32_t* __restrict__ status) {
-  using L = PassSmem<RB, WARPS, ITEMS>;
+template <int RB, int WARPS, int ITEMS, bool STABLE, int SCAN>
+__global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
+    sort_pass_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int n,
+                     int shift, const uint32_t* __restrict__ bin_base,
+                     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter,
+                     const uint32_t* __restrict__ tile_prefix, uint32_t* __restrict__ status,
+                     const uint32_t* __restrict__ gate, const int4* __restrict__ tdesc) {
+  if (gate && *gate == 0) return;
+  using L = PassSmem<RB, WARPS, ITEMS, STABLE>;
   constexpr int BINS = L::BINS, THREADS = WARPS * 32, TILE = L::TILE;
   constexpr uint32_t MASK = BINS - 1;
   extern __shared__ __align__(16) unsigned char smem[];
-  uint16_t* whist = reinterpret_cast<uint16_t*>(smem);  // [WARPS][BINS]
-  uint32_t* stage = reinterpret_cast<uint32_t*>(smem);  // [TILE], aliases whist
+  uint16_t* whist = reinterpret_cast<uint16_t*>(smem);             // STABLE: [WARPS][BINS]
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(smem);               // !STABLE: [BINS]
+  uint32_t* stage = reinterpret_cast<uint32_t*>(smem + (STABLE ? 0 : L::HIST_BYTES));  // [TILE]
   uint32_t* bin_local = reinterpret_cast<uint32_t*>(smem + L::UNION_BYTES);  // [BINS]
   uint32_t* bin_glob = bin_local + BINS;                                      // [BINS]
   uint32_t* misc = bin_glob + BINS;                                           // [64]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) misc[0] = atomicAdd(tile_counter, 1u);
-  for (int i = tid; i < WARPS * BINS / 2; i += THREADS) reinterpret_cast<uint32_t*>(whist)[i] = 0;
+  if (SCAN == 0) {
+    if (tid == 0) misc[0] = atomicAdd(tile_counter, 1u);
+  }
+  if (STABLE) {
+    for (int i = tid; i < WARPS * BINS / 2; i += THREADS) reinterpret_cast<uint32_t*>(whist)[i] = 0;
+  } else {
+    for (int i = tid; i < BINS; i += THREADS) cnt[i] = 0;
+  }
   __syncthreads();
-  const int tile = (int)misc[0];
-  const int tile_start = tile * TILE;
-  const int valid = min(TILE, n - tile_start);
+  const int tile = SCAN == 0 ? (int)misc[0] : (int)blockIdx.x;
+  // Batched sorts pass tile descriptors {first key, end key, cloud, first tile
+  // of the cloud}: a tile never crosses a cloud boundary.
+  const int tile_start = tdesc ? tdesc[tile].x : tile * TILE;
+  const int tile_end = tdesc ? tdesc[tile].y : n;
+  const int valid = min(TILE, tile_end - tile_start);
 
   // Load (warp-striped: item-major within each warp's contiguous segment).
   uint32_t key[ITEMS];
@@ -176,26 +211,39 @@ __global__ void __launch_bounds__(WARPS * 32, 2)
 #pragma unroll
   for (int it = 0; it < ITEMS; ++it) {
     const int idx = wbase + it * 32 + lane;
-    key[it] = idx < n ? __ldcs(src + idx) : 0xffffffffu;
+    key[it] = idx < tile_end ? __ldcs(src + idx) : 0xffffffffu;
   }
 
-  // Warp multi-split ranking, stable in (item, lane) order.
   uint16_t rank[ITEMS];
-  uint16_t* wh = whist + warp * BINS;
-  const uint32_t lt = lanemask_lt();
+  if (STABLE) {
+    uint16_t* wh = whist + warp * BINS;
+    const uint32_t lt = lanemask_lt();
 #pragma unroll
-  for (int it = 0; it < ITEMS; ++it) {
-    const uint32_t d = (key[it] >> shift) & MASK;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t before = wh[d];
-    rank[it] = (uint16_t)(before + __popc(peers & lt));
-    __syncwarp();
-    if ((peers & lt) == 0) wh[d] = (uint16_t)(before + __popc(peers));
-    __syncwarp();
+    for (int it = 0; it < ITEMS; ++it) {
+      const uint32_t d = (key[it] >> shift) & MASK;
+      uint32_t peers = 0xffffffffu;
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+        peers &= ((d >> b) & 1u) ? bal : ~bal;
+      }
+      const uint32_t before = wh[d];
+      rank[it] = (uint16_t)(before + __popc(peers & lt));
+      __syncwarp();
+      if ((peers & lt) == 0) wh[d] = (uint16_t)(before + __popc(peers));
+      __syncwarp();
+    }
+  } else {
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+      const int idx = wbase + it * 32 + lane;
+      rank[it] = idx < tile_end ? (uint16_t)atomicAdd(&cnt[(key[it] >> shift) & MASK], 1u)
+                                : (uint16_t)0;
+    }
   }
   __syncthreads();
 
-  // Per-digit: exclusive offsets across warps, tile count, publish.
+  // Per-digit tile counts (stable: plus exclusive offsets across warps), publish.
   const int invalid = TILE - valid;
   constexpr int PER_T = (BINS + THREADS - 1) / THREADS;
   uint32_t own[PER_T];
@@ -204,15 +252,21 @@ __global__ void __launch_bounds__(WARPS * 32, 2)
     const int b = tid + j * THREADS;
     if (b >= BINS) break;
     uint32_t run = 0;
+    if (STABLE) {
 #pragma unroll
-    for (int w = 0; w < WARPS; ++w) {
-      const uint32_t c = whist[w * BINS + b];
-      whist[w * BINS + b] = (uint16_t)run;
-      run += c;
+      for (int w = 0; w < WARPS; ++w) {
+        const uint32_t c = whist[w * BINS + b];
+        whist[w * BINS + b] = (uint16_t)run;
+        run += c;
+      }
+      own[j] = run - (b == (int)MASK ? (uint32_t)invalid : 0u);  // padding ranks last
+    } else {
+      run = cnt[b];  // padding keys took no rank
+      own[j] = run;
     }
-    bin_local[b] = run;  // tile count including out-of-range padding keys
-    own[j] = run - (b == (int)MASK ? (uint32_t)invalid : 0u);
-    st_release_u32(lookback + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | own[j]);
+    bin_local[b] = run;
+    if (SCAN == 0)
+      st_relaxed_u32(lookback + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | own[j]);
   }
   __syncthreads();
 
@@ -237,70 +291,71 @@ __global__ void __launch_bounds__(WARPS * 32, 2)
   }
   __syncthreads();
 
-  // Decoupled look-back per digit (bounded waits). The first probe reads the
-  // immediate predecessor; past it, a thread loads a window of kWin
-  // predecessor words at once (relaxed loads: flag and count share a word),
-  // so walking back over k tiles that are not yet inclusive costs about
-  // k / kWin round trips. Tiles that start together (the first wave) walk
-  // far; later tiles usually stop at the first probe.
-  constexpr int kWin = 16;
+  if (SCAN == 1) {
+    for (int b = tid; b < BINS; b += THREADS)
+      bin_glob[b] = tile_prefix[(size_t)tile * BINS + b] - bin_local[b];
+  } else {
+    // Decoupled look-back per digit: first probe the immediate predecessor,
+    // then windows of kWin predecessor words (relaxed loads, all in flight).
+    constexpr int kWin = 16;
 #pragma unroll
-  for (int j = 0; j < PER_T; ++j) {
-    const int b = tid + j * THREADS;
-    if (b >= BINS) break;
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      int pred = tile - 1;
-      uint32_t spins = 0;
-      bool done = false;
-      {  // first probe: the immediate predecessor
-        uint32_t w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
-        while ((w0 & kFlagMask) == 0) {
-          if (++spins > kSpinLimit) {
-            raise_status(status, kStatusSpinTimeout);
-            break;
+    for (int j = 0; j < PER_T; ++j) {
+      const int b = tid + j * THREADS;
+      if (b >= BINS) break;
+      uint32_t prefix = 0;
+      if (tile > 0) {
+        int pred = tile - 1;
+        uint32_t spins = 0;
+        bool done = false;
+        {
+          uint32_t w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
+          while ((w0 & kFlagMask) == 0) {
+            if (++spins > kSpinLimit) {
+              raise_status(status, kStatusSpinTimeout);
+              break;
+            }
+            backoff(spins);
+            w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
           }
-          backoff(spins);
-          w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
+          prefix += w0 & kValMask;
+          done = (w0 & kFlagMask) == kFlagInc || spins > kSpinLimit;
+          --pred;
         }
-        prefix += w0 & kValMask;
-        done = (w0 & kFlagMask) == kFlagInc || spins > kSpinLimit;
-        --pred;
-      }
-      while (!done) {
-        uint32_t w[kWin];
+        while (!done) {
+          uint32_t w[kWin];
 #pragma unroll
-        for (int k = 0; k < kWin; ++k)
-          w[k] = (pred - k >= 0) ? ld_relaxed_u32(lookback + (size_t)(pred - k) * BINS + b)
-                                 : kFlagInc;
-        bool stop = false;
-        int adv = 0;
+          for (int k = 0; k < kWin; ++k)
+            w[k] = (pred - k >= 0) ? ld_relaxed_u32(lookback + (size_t)(pred - k) * BINS + b)
+                                   : kFlagInc;
+          bool stop = false;
+          int adv = 0;
 #pragma unroll
-        for (int k = 0; k < kWin; ++k) {
-          const uint32_t f = w[k] & kFlagMask;
-          if (!stop) {
-            if (f == 0) {
-              stop = true;
-            } else {
-              prefix += w[k] & kValMask;
-              ++adv;
-              if (f == kFlagInc) stop = done = true;
+          for (int k = 0; k < kWin; ++k) {
+            const uint32_t f = w[k] & kFlagMask;
+            if (!stop) {
+              if (f == 0) {
+                stop = true;
+              } else {
+                prefix += w[k] & kValMask;
+                ++adv;
+                if (f == kFlagInc) stop = done = true;
+              }
             }
           }
-        }
-        if (done) break;
-        pred -= adv;
-        if (adv < kWin) {  // stopped at a word that is not ready yet: poll it again
-          if (++spins > kSpinLimit) {
-            raise_status(status, kStatusSpinTimeout);
-            break;
+          if (done) break;
+          pred -= adv;
+          if (adv < kWin) {  // stopped at a word that is not ready yet: poll it again
+            if (++spins > kSpinLimit) {
+              raise_status(status, kStatusSpinTimeout);
+              break;
+            }
+            backoff(spins);
           }
-          backoff(spins);
         }
+        st_relaxed_u32(lookback + (size_t)tile * BINS + b, kFlagInc | ((prefix + own[j]) & kValMask));
       }
-      st_release_u32(lookback + (size_t)tile * BINS + b, kFlagInc | ((prefix + own[j]) & kValMask));
+      bin_glob[b] = bin_base[b] + prefix - bin_local[b];
     }
-    bin_glob[b] = bin_base[b] + prefix - bin_local[b];
   }
 
   // Local positions (read before the staging area overwrites the counters).
@@ -308,16 +363,18 @@ __global__ void __launch_bounds__(WARPS * 32, 2)
 #pragma unroll
   for (int it = 0; it < ITEMS; ++it) {
     const uint32_t d = (key[it] >> shift) & MASK;
-    pos[it] = (uint16_t)(bin_local[d] + whist[warp * BINS + d] + rank[it]);
+    pos[it] = (uint16_t)(bin_local[d] + (STABLE ? whist[warp * BINS + d] : 0u) + rank[it]);
   }
   __syncthreads();
 #pragma unroll
-  for (int it = 0; it < ITEMS; ++it) stage[pos[it]] = key[it];
+  for (int it = 0; it < ITEMS; ++it) {
+    if (STABLE || wbase + it * 32 + lane < tile_end) stage[pos[it]] = key[it];
+  }
   __syncthreads();
 
   // Scatter in digit runs; padding keys sit at [valid, TILE) and are skipped.
-#pragma unroll 4
   bool oob = false;
+#pragma unroll 4
   for (int j = tid; j < valid; j += THREADS) {
     const uint32_t k = stage[j];
     const uint32_t g = bin_glob[(k >> shift) & MASK] + (uint32_t)j;
@@ -329,33 +386,112 @@ __global__ void __launch_bounds__(WARPS * 32, 2)
   if (oob) raise_status(status, kStatusSpinTimeout);
 }
 
+// Per-tile digit counts for SCAN 1 passes: th[tile * BINS + b].
+template <int RB>
+__global__ void __launch_bounds__(256)
+    tile_hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tile_keys,
+                     uint32_t* __restrict__ th, const uint32_t* __restrict__ gate,
+                     const int4* __restrict__ tdesc) {
+  if (gate && *gate == 0) return;
+  constexpr int BINS = 1 << RB;
+  __shared__ uint32_t h[BINS];
+  for (int b = threadIdx.x; b < BINS; b += 256) h[b] = 0;
+  __syncthreads();
+  const int t = blockIdx.x;
+  const int lo = tdesc ? tdesc[t].x : t * tile_keys;
+  const int hi = tdesc ? tdesc[t].y : min(n, lo + tile_keys);
+  const bool vec = ((reinterpret_cast<uintptr_t>(keys + lo)) & 15u) == 0;
+  const int n4 = vec ? (hi - lo) >> 2 : 0;
+  const uint4* k4 = reinterpret_cast<const uint4*>(keys + lo);
+  for (int i = threadIdx.x; i < n4; i += 256) {
+    const uint4 v = __ldcs(k4 + i);
+    atomicAdd(&h[(v.x >> shift) & (BINS - 1)], 1u);
+    atomicAdd(&h[(v.y >> shift) & (BINS - 1)], 1u);
+    atomicAdd(&h[(v.z >> shift) & (BINS - 1)], 1u);
+    atomicAdd(&h[(v.w >> shift) & (BINS - 1)], 1u);
+  }
+  for (int i = lo + 4 * n4 + threadIdx.x; i < hi; i += 256)
+    atomicAdd(&h[(keys[i] >> shift) & (BINS - 1)], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < BINS; b += 256) th[(size_t)t * BINS + b] = h[b];
+}
+
+// In place: th[t][b] becomes the output index where tile t's keys of digit b
+// start (bin_base[b] + counts of earlier tiles). Block: 32 digits x 32 tile
+// groups; lanes run along digits, so every load is a coalesced 128 B row part.
+__global__ void __launch_bounds__(1024)
+    tile_scan_kernel(uint32_t* __restrict__ th, int tiles, int bins,
+                     const uint32_t* __restrict__ bin_base, const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
+  __shared__ uint32_t part[32][33];
+  const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int d = blockIdx.x * 32 + l;
+  const int t0 = (int)((long long)tiles * g / 32), t1 = (int)((long long)tiles * (g + 1) / 32);
+  uint32_t sum = 0;
+  if (d < bins) {
+    int t = t0;
+    for (; t + 4 <= t1; t += 4) {
+      const uint32_t a = th[(size_t)t * bins + d], b = th[(size_t)(t + 1) * bins + d];
+      const uint32_t c = th[(size_t)(t + 2) * bins + d], e = th[(size_t)(t + 3) * bins + d];
+      sum += a + b + c + e;
+    }
+    for (; t < t1; ++t) sum += th[(size_t)t * bins + d];
+  }
+  part[g][l] = sum;
+  __syncthreads();
+  if (d >= bins) return;
+  uint32_t run = bin_base[d];
+  for (int k = 0; k < g; ++k) run += part[k][l];
+  for (int t = t0; t < t1; ++t) {
+    const uint32_t v = th[(size_t)t * bins + d];
+    th[(size_t)t * bins + d] = run;
+    run += v;
+  }
+}
+
 // --------------------------------------------------------------------------
 // Host-side planning and launch.
 // --------------------------------------------------------------------------
-template <int RB, int WARPS, int ITEMS>
-static int tiles_for(int n) {
-  constexpr int TILE = WARPS * 32 * ITEMS;
-  return (n + TILE - 1) / TILE;
+static SortConfig g_default_cfg = {10, 16, 16, 1};
+
+void set_sort_config(const SortConfig& c) { g_default_cfg = c; }
+SortConfig get_sort_config() { return g_default_cfg; }
+
+static bool valid_config(const SortConfig& c) {
+  return ((c.radix_bits == 10 && c.warps == 16 && (c.items == 16 || c.items == 24)) ||
+          (c.radix_bits == 8 && c.warps == 16 && (c.items == 16 || c.items == 24))) &&
+         (c.scan == 0 || c.scan == 1);
 }
 
-SortPlan sort_plan(int n, int key_bits) {
+SortPlan sort_plan_cfg(int n, int key_bits, SortConfig cfg) {
+  if (!valid_config(cfg)) cfg = SortConfig{10, 16, 16, 1};
   SortPlan p{};
   p.n = n;
-  p.radix_bits = key_bits <= 30 ? 10 : 8;
+  p.cfg = cfg;
+  // 30-bit keys: the configured digit width; wider keys: 8-bit digits.
+  p.radix_bits = key_bits <= 30 ? cfg.radix_bits : 8;
+  if (p.radix_bits == 8 && cfg.radix_bits != 8) p.cfg.items = 16;
+  p.cfg.radix_bits = p.radix_bits;
   p.passes = (key_bits + p.radix_bits - 1) / p.radix_bits;
   if (p.passes < 1) p.passes = 1;
   p.bins = 1 << p.radix_bits;
-  p.tile = p.radix_bits == 10 ? 16 * 32 * 16 : 16 * 32 * 15;
+  p.tile = p.cfg.warps * 32 * p.cfg.items;
   p.tiles = n > 0 ? (n + p.tile - 1) / p.tile : 0;
-  // control block: hist[passes*bins] + base[passes*bins] + counters[passes]
-  // + lookback[passes*tiles*bins]
+  // zeroed per sort: hist, counters, look-back (scan 0); then base and the
+  // per-tile histograms (scan 1), which are fully written before being read.
   p.hist_off = 0;
-  p.base_off = align_up(p.hist_off + sizeof(uint32_t) * p.passes * p.bins, 256);
-  p.counter_off = align_up(p.base_off + sizeof(uint32_t) * p.passes * p.bins, 256);
+  p.counter_off = align_up(p.hist_off + sizeof(uint32_t) * p.passes * p.bins, 256);
   p.lookback_off = align_up(p.counter_off + sizeof(uint32_t) * 64, 256);
-  p.bytes = align_up(p.lookback_off + sizeof(uint32_t) * (size_t)p.passes * p.tiles * p.bins, 256);
+  const size_t lb_bytes = p.cfg.scan == 0 ? sizeof(uint32_t) * (size_t)p.passes * p.tiles * p.bins : 0;
+  p.zero_bytes = align_up(p.lookback_off + lb_bytes, 256);
+  p.base_off = p.zero_bytes;
+  p.tile_hist_off = align_up(p.base_off + sizeof(uint32_t) * p.passes * p.bins, 256);
+  const size_t th_bytes = p.cfg.scan == 1 ? sizeof(uint32_t) * (size_t)p.tiles * p.bins : 0;
+  p.bytes = align_up(p.tile_hist_off + th_bytes, 256);
   return p;
 }
+
+SortPlan sort_plan(int n, int key_bits) { return sort_plan_cfg(n, key_bits, g_default_cfg); }
 
 static int g_num_sms = 0;
 int device_sm_count() {
@@ -368,20 +504,59 @@ int device_sm_count() {
   return g_num_sms;
 }
 
-template <int RB, int WARPS, int ITEMS>
-static cudaError_t launch_pass(const uint32_t* src, uint32_t* dst, int n, int shift,
-                               const uint32_t* base, uint32_t* lookback, uint32_t* counter,
-                               uint32_t* status, cudaStream_t s) {
-  using L = PassSmem<RB, WARPS, ITEMS>;
-  auto k = onesweep_pass_kernel<RB, WARPS, ITEMS>;
+template <int RB, int WARPS, int ITEMS, bool STABLE, int SCAN>
+static cudaError_t launch_pass_t(const uint32_t* src, uint32_t* dst, int n, int shift,
+                                 const uint32_t* base, uint32_t* lookback, uint32_t* counter,
+                                 const uint32_t* tile_prefix, uint32_t* status,
+                                 const uint32_t* gate, cudaStream_t s, const int4* tdesc,
+                                 int tiles_override) {
+  using L = PassSmem<RB, WARPS, ITEMS, STABLE>;
+  auto k = sort_pass_kernel<RB, WARPS, ITEMS, STABLE, SCAN>;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
     attr = true;
   }
-  const int tiles = tiles_for<RB, WARPS, ITEMS>(n);
-  k<<<tiles, WARPS * 32, L::BYTES, s>>>(src, dst, n, shift, base, lookback, counter, status);
+  const int tiles = tiles_override > 0 ? tiles_override : (n + L::TILE - 1) / L::TILE;
+  k<<<tiles, WARPS * 32, L::BYTES, s>>>(src, dst, n, shift, base, lookback, counter, tile_prefix,
+                                        status, gate, tdesc);
   return cudaGetLastError();
+}
+
+template <int RB, int WARPS, int ITEMS>
+static cudaError_t launch_pass_cfg(bool stable, int scan, const uint32_t* src, uint32_t* dst,
+                                   int n, int shift, const uint32_t* base, uint32_t* lookback,
+                                   uint32_t* counter, const uint32_t* tile_prefix,
+                                   uint32_t* status, const uint32_t* gate, cudaStream_t s,
+                                   const int4* tdesc, int tiles) {
+  if (stable)
+    return scan == 0 ? launch_pass_t<RB, WARPS, ITEMS, true, 0>(src, dst, n, shift, base, lookback,
+                                                                 counter, tile_prefix, status, gate, s, tdesc, tiles)
+                     : launch_pass_t<RB, WARPS, ITEMS, true, 1>(src, dst, n, shift, base, lookback,
+                                                                 counter, tile_prefix, status, gate, s, tdesc, tiles);
+  return scan == 0 ? launch_pass_t<RB, WARPS, ITEMS, false, 0>(src, dst, n, shift, base, lookback,
+                                                                counter, tile_prefix, status, gate, s, tdesc, tiles)
+                   : launch_pass_t<RB, WARPS, ITEMS, false, 1>(src, dst, n, shift, base, lookback,
+                                                                counter, tile_prefix, status, gate, s, tdesc, tiles);
+}
+
+cudaError_t launch_pass(const SortPlan& p, bool stable, const uint32_t* src, uint32_t* dst,
+                        int shift, const uint32_t* base, uint32_t* lookback, uint32_t* counter,
+                        const uint32_t* tile_prefix, uint32_t* status, const uint32_t* gate,
+                        cudaStream_t s, const int4* tdesc, int tiles) {
+  const int sc = p.cfg.scan;
+  if (p.radix_bits == 10) {
+    if (p.cfg.items == 24)
+      return launch_pass_cfg<10, 16, 24>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
+                                         tile_prefix, status, gate, s, tdesc, tiles);
+    return launch_pass_cfg<10, 16, 16>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
+                                       tile_prefix, status, gate, s, tdesc, tiles);
+  }
+  if (p.cfg.items == 24)
+    return launch_pass_cfg<8, 16, 24>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
+                                      tile_prefix, status, gate, s, tdesc, tiles);
+  return launch_pass_cfg<8, 16, 16>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
+                                    tile_prefix, status, gate, s, tdesc, tiles);
 }
 
 cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float min_coord,
@@ -407,8 +582,8 @@ cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float 
   return cudaGetLastError();
 }
 
-cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* ctrl,
-                             cudaStream_t s) {
+cudaError_t launch_histogram_gated(const uint32_t* keys, const SortPlan* plan, void* ctrl,
+                                   const uint32_t* gate, cudaStream_t s) {
   if (plan->n <= 0) return cudaSuccess;
   uint32_t* hist = reinterpret_cast<uint32_t*>(static_cast<char*>(ctrl) + plan->hist_off);
   const size_t sm = sizeof(uint32_t) * plan->passes * plan->bins;
@@ -416,17 +591,20 @@ cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* c
   int need = (plan->n / 4 + 255) / 256 + 1;
   const int grid = need < blocks ? need : blocks;
   if (plan->radix_bits == 10)
-    histogram_kernel<10><<<grid, 256, sm, s>>>(keys, plan->n, hist, plan->passes);
+    histogram_kernel<10><<<grid, 256, sm, s>>>(keys, plan->n, hist, plan->passes, gate);
   else
-    histogram_kernel<8><<<grid, 256, sm, s>>>(keys, plan->n, hist, plan->passes);
+    histogram_kernel<8><<<grid, 256, sm, s>>>(keys, plan->n, hist, plan->passes, gate);
   return cudaGetLastError();
 }
 
-// Runs the digit passes (histograms must already be in the control block).
-// Keys move src -> alt -> src ...; returns which buffer holds the result.
-cudaError_t launch_sort_passes(uint32_t* keys, uint32_t* alt, const SortPlan* plan, void* ctrl,
-                               uint32_t* status, cudaStream_t s, uint32_t** result,
-                               Recorder* rec) {
+cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* ctrl,
+                             cudaStream_t s) {
+  return launch_histogram_gated(keys, plan, ctrl, nullptr, s);
+}
+
+static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
+                                    void* ctrl, uint32_t* status, const uint32_t* gate,
+                                    cudaStream_t s, uint32_t** result, Recorder* rec) {
   *result = keys;
   if (plan->n <= 1) return cudaSuccess;
   char* c = static_cast<char*>(ctrl);
@@ -434,23 +612,31 @@ cudaError_t launch_sort_passes(uint32_t* keys, uint32_t* alt, const SortPlan* pl
   uint32_t* base = reinterpret_cast<uint32_t*>(c + plan->base_off);
   uint32_t* counters = reinterpret_cast<uint32_t*>(c + plan->counter_off);
   uint32_t* lookback = reinterpret_cast<uint32_t*>(c + plan->lookback_off);
+  uint32_t* th = reinterpret_cast<uint32_t*>(c + plan->tile_hist_off);
   if (plan->radix_bits == 10)
-    hist_scan_kernel<10><<<plan->passes, 1024, 0, s>>>(hist, base);
+    hist_scan_kernel<10><<<plan->passes, 1024, 0, s>>>(hist, base, gate);
   else
-    hist_scan_kernel<8><<<plan->passes, 256, 0, s>>>(hist, base);
+    hist_scan_kernel<8><<<plan->passes, 256, 0, s>>>(hist, base, gate);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(rec, s);
   uint32_t* a = keys;
   uint32_t* b = alt;
   for (int p = 0; p < plan->passes; ++p) {
+    const int shift = p * plan->radix_bits;
+    if (plan->cfg.scan == 1) {
+      if (plan->radix_bits == 10)
+        tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gate,
+                                                         nullptr);
+      else
+        tile_hist_kernel<8><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gate,
+                                                        nullptr);
+      tile_scan_kernel<<<(plan->bins + 31) / 32, 1024, 0, s>>>(th, plan->tiles, plan->bins,
+                                                               base + p * plan->bins, gate);
+    }
     uint32_t* lb = lookback + (size_t)p * plan->tiles * plan->bins;
-    if (plan->radix_bits == 10)
-      e = launch_pass<10, 16, 16>(a, b, plan->n, p * 10, base + p * plan->bins, lb, counters + p,
-                                  status, s);
-    else
-      e = launch_pass<8, 16, 15>(a, b, plan->n, p * 8, base + p * plan->bins, lb, counters + p,
-                                 status, s);
+    e = launch_pass(*plan, p > 0, a, b, shift, base + p * plan->bins,
+                    plan->cfg.scan == 0 ? lb : nullptr, counters + p, th, status, gate, s, nullptr, 0);
     if (e != cudaSuccess) return e;
     mark(rec, s);
     uint32_t* t = a;
@@ -459,6 +645,27 @@ cudaError_t launch_sort_passes(uint32_t* keys, uint32_t* alt, const SortPlan* pl
   }
   *result = a;
   return cudaSuccess;
+}
+
+cudaError_t launch_sort_passes(uint32_t* keys, uint32_t* alt, const SortPlan* plan, void* ctrl,
+                               uint32_t* status, cudaStream_t s, uint32_t** result,
+                               Recorder* rec) {
+  return sort_passes_impl(keys, alt, plan, ctrl, status, nullptr, s, result, rec);
+}
+
+cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
+                                     void* ctrl, uint32_t* status, const uint32_t* gate,
+                                     cudaStream_t s, uint32_t** result) {
+  return sort_passes_impl(keys, alt, plan, ctrl, status, gate, s, result, nullptr);
+}
+
+cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
+                             const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s) {
+  if (radix_bits == 10)
+    tile_hist_kernel<10><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc);
+  else
+    tile_hist_kernel<8><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc);
+  return cudaGetLastError();
 }
 
 }  // namespace octgb

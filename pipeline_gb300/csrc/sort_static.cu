@@ -90,7 +90,7 @@ OCT_API int oct_sort_keys_noalloc(uint32_t* keys, uint32_t* keys_alt, int n, int
   }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   // The array keeps the previous call's counters and flags: clear them.
-  e = cudaMemsetAsync(scratch, 0, p.bytes, s);
+  e = cudaMemsetAsync(scratch, 0, p.zero_bytes, s);
   if (e == cudaSuccess) e = launch_histogram(keys, &p, scratch, s);
   uint32_t* result = keys;
   if (e == cudaSuccess) e = launch_sort_passes(keys, keys_alt, &p, scratch, d_status, s, &result);

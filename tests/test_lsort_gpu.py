@@ -1,0 +1,132 @@
+"""Learned bucketed sort + unique, and the whole learned build: bit-exact with
+the plain path / the oracle; fallback exact; the trained model's gain over
+plain key-space bucketing on clustered keys."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def dev_keys(a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+
+
+def fitted(keys_np, n_buckets=4096, segments=4096, steps=100, sample=1 << 18, seed=0):
+    from pipeline_gb300.learned import LearnedCDF
+
+    rng = np.random.default_rng(seed)
+    samp = keys_np[rng.integers(0, len(keys_np), min(sample, len(keys_np)))]
+    m = LearnedCDF(max_segments=segments)
+    m.fit(dev_keys(samp), n_segments=segments, steps=steps, n_buckets=n_buckets)
+    return m
+
+
+def no_model(n_buckets=4096):
+    """Key-space bucketing: one segment [0, 2^30) with a linear CDF (top key bits)."""
+    from pipeline_gb300.learned import LearnedCDF
+
+    m = LearnedCDF(max_segments=4)
+    m.fit(dev_keys(np.array([0, (1 << 30) - 1], np.uint32)), n_segments=1, steps=0,
+          n_buckets=n_buckets)
+    return m
+
+
+def clustered_keys(n, seed=3):
+    from pipeline_gb300 import datasets
+
+    pts = datasets.gaussian_mixture(n, 64, np.random.default_rng(seed), noise=0.05)
+    return O.morton(pts, 0.0, 1024.0, threads=4)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "clustered"])
+@pytest.mark.parametrize("n", [1, 5000, 1 << 20])
+def test_lsort_unique_exact(kind, n):
+    from pipeline_gb300.pipeline import lsort_unique
+
+    if kind == "uniform":
+        keys = np.random.default_rng(n).integers(0, 1 << 30, n).astype(np.uint32)
+    else:
+        keys = clustered_keys(n)
+    m = fitted(keys, n_buckets=1024 if n < 100000 else 4096)
+    out, stats = lsort_unique(dev_keys(keys), m)
+    assert out.cpu().numpy().view(np.uint32).tobytes() == np.unique(keys).tobytes()
+    assert stats["fallback"] == 0, stats
+
+
+def test_lsort_forced_fallback_is_exact():
+    from pipeline_gb300.pipeline import lsort_unique
+
+    keys = clustered_keys(1 << 20)
+    m = fitted(keys)
+    out, stats = lsort_unique(dev_keys(keys), m, overflow_threshold=-1.0)
+    assert stats["fallback"] == 1 and stats["skip"] == 1
+    assert out.cpu().numpy().view(np.uint32).tobytes() == np.unique(keys).tobytes()
+
+
+def test_trained_model_balances_buckets_where_key_bits_do_not():
+    """What the trained CDF gains over bucketing by key bits on clustered keys:
+    the largest bucket and the share of keys in oversized buckets."""
+    from pipeline_gb300.pipeline import lsort_unique
+
+    keys = clustered_keys(1 << 22)
+    trained = fitted(keys)
+    plain = no_model()
+    out_t, st_t = lsort_unique(dev_keys(keys), trained, overflow_threshold=1.0)
+    out_p, st_p = lsort_unique(dev_keys(keys), plain, overflow_threshold=1.0)
+    want = np.unique(keys).tobytes()
+    assert out_t.cpu().numpy().view(np.uint32).tobytes() == want
+    assert out_p.cpu().numpy().view(np.uint32).tobytes() == want
+    avg = len(keys) / 4096
+    assert st_t["fallback"] == 0, st_t
+    assert st_t["max_bucket"] < 8 * avg, st_t
+    assert st_p["max_bucket"] > 10 * st_t["max_bucket"], (st_p, st_t)
+    assert st_t["overflow_frac"] < 0.05 < st_p["overflow_frac"], (st_t, st_p)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "clustered"])
+def test_learned_build_matches_oracle(kind):
+    from pipeline_gb300 import datasets
+    from pipeline_gb300.pipeline import LearnedOctreeBuilder
+
+    n = 1 << 20
+    if kind == "uniform":
+        pts = O.init_random_vec4(n)
+    else:
+        pts = datasets.gaussian_mixture(n, 64, np.random.default_rng(9), noise=0.05)
+    keys = O.morton(pts, 0.0, 1024.0)
+    m = fitted(keys)
+    b = LearnedOctreeBuilder(n, m)
+    b.build(torch.from_numpy(pts).cuda(), 0.0, 1024.0)
+    res = b.result()
+    want = O.build_all(pts, 0.0, 1024.0, threads=4)
+    assert (res["n_unique"], res["n_oct"], res["status"]) == (want["n_unique"], want["n_oct"], 0)
+    for key in ["sorted_unique", "prefix_n", "has_leaf_left", "has_leaf_right", "left_child",
+                "parent", "edge_count", "prefix_sum", "oct_nodes"]:
+        assert res[key].tobytes() == np.asarray(want[key]).tobytes(), key
+    assert b.lsort_stats()["fallback"] == 0
+
+
+@pytest.mark.parametrize("cfg", [(10, 16, 16, 0), (10, 16, 16, 1), (10, 16, 24, 1), (8, 16, 16, 0),
+                                 (8, 16, 24, 1)])
+def test_every_sort_config_sorts(cfg):
+    from pipeline_gb300 import _lib
+    from pipeline_gb300.kernels import k_SimpleRadixSort
+
+    import ctypes
+
+    lib = _lib.load()
+    old = (ctypes.c_int * 4)()
+    lib.oct_get_sort_config(old)
+    try:
+        assert lib.oct_set_sort_config(*cfg) == 0
+        rng = np.random.default_rng(sum(cfg))
+        for n, bits in [(1_000_003, 30), (300_001, 32), (7, 30)]:
+            a = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+            keys = dev_keys(a)
+            k_SimpleRadixSort(keys, n, key_bits=bits)
+            assert keys.cpu().numpy().view(np.uint32).tobytes() == np.sort(a).tobytes(), (cfg, n, bits)
+    finally:
+        lib.oct_set_sort_config(*list(old))
