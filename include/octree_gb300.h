@@ -262,10 +262,13 @@ OCT_API int oct_build_octree_timed(const oct_vec4* points, int n, float min_coor
 /* come from exact fixed-point tables and never decrease with the key.       */
 /* ----------------------------------------------------------------------- */
 #define OCT_LCDF_MAX_SEGMENTS 4096
+#define OCT_LCDF_MAX_BUCKETS 65536
 /* Byte offsets of the model's parts: {x, theta, adam_m, adam_v, y, grad, yq,
- * slope, lut, total}; x is uint32[K+1], theta/adam/y/grad float, yq uint32[K+1],
- * slope uint64[K], lut uint32[4097]. */
-OCT_API int oct_lcdf_layout(int max_segments, size_t offsets[10]);
+ * slope, lut, bounds, blut, total}; x is uint32[K+1], theta/adam/y/grad float,
+ * yq uint32[K+1], slope uint64[K], lut uint16[4097] (knots below each 2^18-key
+ * cell), bounds uint32[NB+1] (smallest key of each bucket, 2^30 past the
+ * last), blut uint16[16385] (bucket at the start of each 2^16-key cell). */
+OCT_API int oct_lcdf_layout(int max_segments, size_t offsets[12]);
 OCT_API size_t oct_lcdf_fit_workspace_bytes(int n_sample);
 /* Sorts the sample into the workspace, places knots, runs `steps` Adam steps
  * (learning rate lr) and builds bucket tables for n_buckets (<= 65536). */
@@ -291,8 +294,9 @@ OCT_API int oct_lcdf_buckets(const void* model, int max_segments, const uint32_t
  * and de-duplicated in shared memory; when more than overflow_threshold of the
  * keys sit in oversized buckets, or a bucket fits no shared-memory form, the
  * same launches fall back to the OneSweep sort + unique (device-side switch).
- * d_stats (nullable, 32 bytes): {fallback, failed_buckets, overflow_keys,
- * max_bucket, n, overflow_frac (float), skip, 0}. On the fallback path `keys`
+ * d_stats (nullable, 48 bytes): {fallback, failed_buckets, overflow_keys,
+ * max_bucket, n, overflow_frac (float), skip, bitmap_buckets, radix_buckets,
+ * bitonic_buckets, 0, 0}. On the fallback path `keys`
  * is sorted in place; otherwise it is left as it was. */
 OCT_API size_t oct_lsort_workspace_bytes(int n, int n_buckets, int max_segments);
 OCT_API int oct_lsort_unique(uint32_t* keys, int n, const void* model, int max_segments,

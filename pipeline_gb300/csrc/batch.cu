@@ -279,8 +279,8 @@ __global__ void __launch_bounds__(256)
     const int nb = max(unique_c[c] - 1, 0);
     const int i = g - cs;
     if (i < nb)
-      radix_node(i, nb, codes + cs, prefix_n + cs, hll + cs, hlr + cs, left_child + cs,
-                 parent + cs);
+      radix_node(i, nb, GlobalCodes{codes + cs}, prefix_n + cs, hll + cs, hlr + cs,
+                 left_child + cs, parent + cs);
   }
 }
 

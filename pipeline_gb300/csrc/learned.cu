@@ -39,7 +39,9 @@ LcdfLayout lcdf_layout(int max_knots) {
   L.g = take(4 * (K + 1));
   L.yq = take(4 * (K + 1));
   L.slope = take(8 * K);
-  L.lut = take(4 * (kLcdfLutSize + 1));
+  L.lut = take(2 * (kLcdfLutSize + 1));
+  L.bounds = take(4 * ((size_t)kLcdfMaxBuckets + 1));
+  L.blut = take(2 * ((size_t)kLcdfBlutSize + 1));
   L.bytes = o;
   return L;
 }
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(1024) lcdf_tables_kernel(char* blob, LcdfLayou
   const float* y = reinterpret_cast<const float*>(blob + L.y);
   uint32_t* yq = reinterpret_cast<uint32_t*>(blob + L.yq);
   unsigned long long* slope = reinterpret_cast<unsigned long long*>(blob + L.slope);
-  uint32_t* lut = reinterpret_cast<uint32_t*>(blob + L.lut);
+  uint16_t* lut = reinterpret_cast<uint16_t*>(blob + L.lut);
   const uint32_t top = (uint32_t)nb << kLcdfFix;
   // Yq_k = round(y_k * NB * 2^16), then a running max keeps it non-decreasing.
   constexpr int PER = (kLcdfMaxKnots + 1023) / 1024;
@@ -332,9 +334,51 @@ __global__ void __launch_bounds__(1024) lcdf_tables_kernel(char* blob, LcdfLayou
       if (x[mid] <= v) lo = mid + 1;
       else hi = mid;
     }
-    lut[p] = (uint32_t)lo;
+    lut[p] = (uint16_t)lo;
   }
   if (threadIdx.x == 0) h->n_buckets = nb;
+}
+
+// Bucket boundaries of the fixed-point model, for the bucketed sort:
+// bounds[b] = smallest key v with bucket(v) >= b (bounds[0] = 0; 2^30 when no
+// key reaches b; bounds[nb] = 2^30), and blut[p] = bucket(p << 16) for the
+// 2^14 cells of 2^16 keys (blut[2^14] = bucket(2^30 - 1)). Because bucket()
+// never decreases, bucket(v) = the largest b with bounds[b] <= v, and that b
+// lies in [blut[v >> 16], blut[(v >> 16) + 1]].
+__global__ void __launch_bounds__(256) lcdf_bounds_kernel(char* blob, LcdfLayout L, int nb) {
+  const LcdfTables t = lcdf_tables_global(blob, L);
+  uint32_t* bounds = reinterpret_cast<uint32_t*>(blob + L.bounds);
+  uint16_t* blut = reinterpret_cast<uint16_t*>(blob + L.blut);
+  const int items = nb + 1 + kLcdfBlutSize + 1;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < items; it += gridDim.x * blockDim.x) {
+    if (it <= nb) {
+      const uint32_t b = (uint32_t)it;
+      uint32_t v;
+      if (b == 0) {
+        v = 0;
+      } else if (b == (uint32_t)nb || lcdf_bucket(t, kLcdfKeyEnd - 1u) < b) {
+        v = kLcdfKeyEnd;
+      } else {
+        uint32_t lo = 0, hi = kLcdfKeyEnd - 1u;  // bucket(hi) >= b
+        while (lo < hi) {
+          const uint32_t mid = lo + ((hi - lo) >> 1);
+          if (lcdf_bucket(t, mid) >= b) hi = mid;
+          else lo = mid + 1;
+        }
+        v = lo;
+      }
+      bounds[b] = v;
+    } else {
+      const int p = it - (nb + 1);
+      const uint32_t v = min((uint32_t)p << (30 - kLcdfBlutBits), kLcdfKeyEnd - 1u);
+      blut[p] = (uint16_t)lcdf_bucket(t, v);
+    }
+  }
+}
+
+static void launch_lcdf_bounds(char* blob, const LcdfLayout& L, int nb, cudaStream_t s) {
+  const int items = nb + 1 + kLcdfBlutSize + 1;
+  lcdf_bounds_kernel<<<(items + 255) / 256, 256, 0, s>>>(blob, L, nb);
 }
 
 // ------------------------------------------------------------- inference --
@@ -375,6 +419,7 @@ cudaError_t launch_lcdf_fit(const uint32_t* sorted_sample, int S, int k_req, int
   lcdf_prep_kernel<<<1, 1024, 0, s>>>(blob, L);
   lcdf_fwd_bwd_kernel<<<grid, 256, fb_smem, s>>>(sorted_sample, S, blob, L);
   lcdf_tables_kernel<<<1, 1024, 0, s>>>(blob, L, nb);
+  launch_lcdf_bounds(blob, L, nb, s);
   return cudaGetLastError();
 }
 
@@ -415,6 +460,7 @@ cudaError_t launch_lcdf_loss_grad(const uint32_t* sorted_sample, int S, char* bl
 cudaError_t launch_lcdf_tables(char* blob, const LcdfLayout& L, int nb, cudaStream_t s) {
   lcdf_prep_kernel<<<1, 1024, 0, s>>>(blob, L);
   lcdf_tables_kernel<<<1, 1024, 0, s>>>(blob, L, nb);
+  launch_lcdf_bounds(blob, L, nb, s);
   return cudaGetLastError();
 }
 
@@ -439,12 +485,13 @@ cudaError_t launch_lcdf_buckets(const char* blob, const LcdfLayout& L, const uin
 // ------------------------------------------------------------------ C ABI --
 extern "C" {
 
-OCT_API int oct_lcdf_layout(int max_segments, size_t offsets[10]) {
+OCT_API int oct_lcdf_layout(int max_segments, size_t offsets[12]) {
   using namespace octgb;
   if (max_segments < 1 || max_segments > kLcdfMaxSegments || !offsets) return OCT_ERR_INVALID_ARG;
   const LcdfLayout L = lcdf_layout(max_segments);
-  const size_t v[10] = {L.x, L.theta, L.adam_m, L.adam_v, L.y, L.g, L.yq, L.slope, L.lut, L.bytes};
-  for (int i = 0; i < 10; ++i) offsets[i] = v[i];
+  const size_t v[12] = {L.x,   L.theta, L.adam_m, L.adam_v, L.y,    L.g,
+                        L.yq,  L.slope, L.lut,    L.bounds, L.blut, L.bytes};
+  for (int i = 0; i < 12; ++i) offsets[i] = v[i];
   return OCT_OK;
 }
 
@@ -460,7 +507,7 @@ OCT_API int oct_lcdf_fit(const uint32_t* sample_keys, int n_sample, int n_segmen
   using namespace octgb;
   if (!sample_keys || !model || !workspace || n_sample < 1 || n_sample > OCT_MAX_N ||
       n_segments < 1 || n_segments > max_segments || max_segments > kLcdfMaxSegments ||
-      steps < 0 || n_buckets < 1 || n_buckets > 65536 || (reinterpret_cast<uintptr_t>(workspace) & 255))
+      steps < 0 || n_buckets < 1 || n_buckets > kLcdfMaxBuckets || (reinterpret_cast<uintptr_t>(workspace) & 255))
     return OCT_ERR_INVALID_ARG;
   if (workspace_bytes < oct_lcdf_fit_workspace_bytes(n_sample)) return OCT_ERR_WORKSPACE;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -503,7 +550,7 @@ OCT_API int oct_lcdf_loss_grad(const uint32_t* sorted_sample, int n_sample, void
 OCT_API int oct_lcdf_tables(void* model, int max_segments, int n_buckets, oct_stream_t stream) {
   using namespace octgb;
   if (!model || max_segments < 1 || max_segments > kLcdfMaxSegments || n_buckets < 1 ||
-      n_buckets > 65536)
+      n_buckets > kLcdfMaxBuckets)
     return OCT_ERR_INVALID_ARG;
   const LcdfLayout L = lcdf_layout(max_segments);
   cudaError_t e = launch_lcdf_tables(static_cast<char*>(model), L, n_buckets,

@@ -11,8 +11,13 @@ constexpr int kLcdfLutBits = 12;
 constexpr int kLcdfLutSize = 1 << kLcdfLutBits;
 constexpr uint32_t kLcdfKeyEnd = 1u << 30;
 constexpr int kLcdfFix = 16;
+constexpr int kLcdfMaxBuckets = 65536;
+// Bucket lookup used by the bucketed sort: the exact bucket boundaries plus a
+// 2^14-entry table of the bucket at the start of each 2^16-key cell.
+constexpr int kLcdfBlutBits = 14;
+constexpr int kLcdfBlutSize = 1 << kLcdfBlutBits;
 constexpr uint32_t kLcdfMagic = 0x4643444cu;  // "LDCF"
-constexpr uint32_t kLcdfVersion = 1;
+constexpr uint32_t kLcdfVersion = 2;
 
 // Blob header (first 256 bytes of a model buffer; persisted with the model).
 struct LcdfHeader {
@@ -29,7 +34,7 @@ struct LcdfHeader {
 
 struct LcdfLayout {
   int max_knots;
-  size_t x, theta, adam_m, adam_v, y, g, yq, slope, lut, bytes;
+  size_t x, theta, adam_m, adam_v, y, g, yq, slope, lut, bounds, blut, bytes;
 };
 
 LcdfLayout lcdf_layout(int max_knots);
@@ -59,13 +64,13 @@ __device__ __forceinline__ LcdfTables lcdf_load_tables(const char* blob, const L
   const uint32_t* x = reinterpret_cast<const uint32_t*>(blob + L.x);
   const uint32_t* yq = reinterpret_cast<const uint32_t*>(blob + L.yq);
   const unsigned long long* slope = reinterpret_cast<const unsigned long long*>(blob + L.slope);
-  const uint32_t* lut = reinterpret_cast<const uint32_t*>(blob + L.lut);
+  const uint16_t* lut = reinterpret_cast<const uint16_t*>(blob + L.lut);
   for (int k = threadIdx.x; k <= K; k += blockDim.x) {
     sx[k] = x[k];
     syq[k] = yq[k];
     if (k < K) sslope[k] = slope[k];
   }
-  for (int p = threadIdx.x; p <= kLcdfLutSize; p += blockDim.x) slut[p] = (uint16_t)lut[p];
+  for (int p = threadIdx.x; p <= kLcdfLutSize; p += blockDim.x) slut[p] = lut[p];
   __syncthreads();
   LcdfTables t;
   t.x = sx;
@@ -73,6 +78,19 @@ __device__ __forceinline__ LcdfTables lcdf_load_tables(const char* blob, const L
   t.slope = sslope;
   t.lut = slut;
   t.K = K;
+  t.nb = h->n_buckets;
+  return t;
+}
+
+// The same tables read in place from the model buffer (global memory).
+__device__ __forceinline__ LcdfTables lcdf_tables_global(const char* blob, const LcdfLayout& L) {
+  const LcdfHeader* h = reinterpret_cast<const LcdfHeader*>(blob);
+  LcdfTables t;
+  t.x = reinterpret_cast<const uint32_t*>(blob + L.x);
+  t.yq = reinterpret_cast<const uint32_t*>(blob + L.yq);
+  t.slope = reinterpret_cast<const unsigned long long*>(blob + L.slope);
+  t.lut = reinterpret_cast<const uint16_t*>(blob + L.lut);
+  t.K = h->n_knots;
   t.nb = h->n_buckets;
   return t;
 }

@@ -6,20 +6,28 @@
 //
 //   hist     per-chunk bucket counts (Morton fused when starting from points)
 //   offsets  per-bucket totals and per-chunk offsets; bucket starts; overflow
-//            fraction (keys in buckets above the shared-memory capacity) and
-//            the fallback decision when it exceeds the threshold
+//            fraction (keys in buckets above the bitonic capacity) and the
+//            fallback decision when it exceeds the threshold
 //   scatter  each chunk writes its keys into its reserved bucket ranges
 //   buckets  one CTA per bucket: the sorted unique keys of the bucket from a
-//            shared-memory bitmap over [min, max] of its keys when that span
-//            fits (any key count), else a bitonic sort of the keys in shared
-//            memory (up to kCap keys); decoupled look-back across buckets
-//            gives each bucket's output offset.
+//            shared-memory bitmap over [min, max] of its keys when that is
+//            dense enough, else a radix sort (or, above the cache size, a
+//            bitonic sort) of its keys in shared memory; the run overwrites
+//            the front of the bucket's own range, its length goes to a table
+//   pack     a scan of the run lengths and one copy per bucket assemble the
+//            output (no bucket ever waits on another)
 //
-// If any bucket fits neither form, or the overflow fraction exceeds the
-// threshold, the device flag `fallback` is set and the OneSweep sort + unique
-// (launched right after, gated on the flag) redo stages 2-3 from the original
-// keys; otherwise those launches return at once. Either way the output is the
-// sorted unique key array, identical to the plain path's.
+// Bucket ids come from the model's boundary table (the smallest key of every
+// bucket) narrowed by a 2^14-entry table over the top key bits, both staged
+// in shared memory; that is the model's own fixed-point bucket function,
+// evaluated without its per-key knot search and 64-bit multiply.
+//
+// If any bucket fits neither form, the overflow fraction exceeds the
+// threshold, or the model's tables were built for another bucket count, the
+// device flag `fallback` is set and the OneSweep sort + unique (launched right
+// after, gated on the flag) redo stages 2-3 from the original keys; otherwise
+// those launches return at once. Either way the output is the sorted unique
+// key array, identical to the plain path's.
 #include <stdio.h>
 
 #include "learned.cuh"
@@ -27,42 +35,109 @@
 
 namespace octgb {
 
-constexpr int kBmBits = 1 << 19;          // bitmap span limit (64 KiB of shared memory)
-constexpr int kBmWords = kBmBits / 32;
-constexpr int kCap = 16384;               // bitonic-sort capacity (keys; the 64 KiB buffer)
-constexpr int kBucketThreads = 512;
+constexpr int kLsThreads = 1024;          // histogram / scatter CTAs (2 per SM)
+constexpr int kLsUnroll = 4;              // keys per thread in flight
+constexpr int kBkThreads = 512;           // bucket CTAs (3 per SM)
+constexpr int kBkWarps = kBkThreads / 32;
+constexpr int kBkWords = 16384;           // 64 KiB working region per bucket CTA
+constexpr int kBkCache = 8192;            // keys cached in the first half (cnt <= kBkCache)
+constexpr int kBkItems = kBkCache / kBkThreads;  // keys per thread in the radix sort
+constexpr uint32_t kBmSmall = 1u << 18;   // bitmap span in the second half (32 KiB)
+constexpr uint32_t kBmBig = 1u << 19;     // bitmap span over the whole region (64 KiB)
+constexpr int kCap = kBkWords;            // bitonic capacity (keys)
+constexpr int kRsBits = 8;                // radix-sort digit width
+constexpr int kRsBins = 1 << kRsBits;
+
+// ------------------------------------------------------- bucket lookup --
+struct BucketLookup {
+  const uint32_t* bounds;  // [nb] smallest key of each bucket
+  const uint16_t* blut;    // [2^14 + 1] bucket at the start of each 2^16-key cell
+  uint32_t last;           // nb - 1
+};
+
+// Stage the lookup tables in shared memory (all threads; ends with a barrier).
+__device__ __forceinline__ BucketLookup load_lookup(const char* __restrict__ blob,
+                                                    const LcdfLayout& L, int nb,
+                                                    uint32_t* s_bounds, uint16_t* s_blut) {
+  const uint32_t* gb = reinterpret_cast<const uint32_t*>(blob + L.bounds);
+  const uint32_t* gl = reinterpret_cast<const uint32_t*>(blob + L.blut);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s_bounds[b] = gb[b];
+  uint32_t* sl = reinterpret_cast<uint32_t*>(s_blut);
+  for (int p = threadIdx.x; p < kLcdfBlutSize / 2; p += blockDim.x) sl[p] = gl[p];
+  if (threadIdx.x == 0)
+    s_blut[kLcdfBlutSize] = reinterpret_cast<const uint16_t*>(blob + L.blut)[kLcdfBlutSize];
+  __syncthreads();
+  return BucketLookup{s_bounds, s_blut, (uint32_t)(nb - 1)};
+}
+
+// bucket(v): the largest b with bounds[b] <= v, searched in
+// [blut[v >> 16], blut[(v >> 16) + 1]], clamped to nb - 1.
+__device__ __forceinline__ uint32_t bucket_of(const BucketLookup& q, uint32_t v) {
+  const uint32_t vc = min(v, kLcdfKeyEnd - 1u);
+  const uint32_t p = vc >> (30 - kLcdfBlutBits);
+  uint32_t hi = min((uint32_t)q.blut[p + 1], q.last);
+  uint32_t lo = min((uint32_t)q.blut[p], hi);
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (q.bounds[mid] <= vc) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+size_t lsort_hist_smem(int nb, int /*max_segments*/) {
+  return align_up(8 * (size_t)nb + 2 * ((size_t)kLcdfBlutSize + 1), 16);
+}
 
 // ------------------------------------------------------------- histogram --
 template <bool FROM_POINTS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kLsThreads, 2)
     lsort_hist_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, int n,
                       float min_coord, float range, const char* __restrict__ blob, LcdfLayout L,
                       uint32_t* __restrict__ chunk_hist, int nb, uint32_t* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* s_hist = reinterpret_cast<uint32_t*>(sm);
-  LcdfTables t = lcdf_load_tables(blob, L, sm + align_up(4 * (size_t)nb, 16));
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0;
-  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += kLsThreads) s_hist[b] = 0;
+  const BucketLookup q = load_lookup(blob, L, nb, s_hist + nb,
+                                     reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
   const int G = gridDim.x, c = blockIdx.x;
   const int lo = (int)((long long)n * c / G), hi = (int)((long long)n * (c + 1) / G);
   bool bad = false;
-  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    uint32_t code;
+  constexpr int U = FROM_POINTS ? 2 : kLsUnroll;  // float4 points: 2 in flight fit 32 registers
+  for (int base = lo + threadIdx.x; base < hi; base += U * kLsThreads) {
+    uint32_t code[U];
     if (FROM_POINTS) {
-      const float4 p = ld_stream_f4(pts + i);
-      bad |= !(in_range(p.x, min_coord, range) && in_range(p.y, min_coord, range) &&
-               in_range(p.z, min_coord, range));
-      code = morton_code(p.x, p.y, p.z, min_coord, range);
-      keys[i] = code;
+      float4 p[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * kLsThreads;
+        if (i < hi) p[u] = ld_stream_f4(pts + i);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * kLsThreads;
+        if (i < hi) {
+          bad |= !(in_range(p[u].x, min_coord, range) && in_range(p[u].y, min_coord, range) &&
+                   in_range(p[u].z, min_coord, range));
+          code[u] = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range);
+          keys[i] = code[u];
+        }
+      }
     } else {
-      code = keys[i];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * kLsThreads;
+        if (i < hi) code[u] = keys[i];
+      }
     }
-    atomicAdd(&s_hist[min(lcdf_bucket(t, code), (uint32_t)(nb - 1))], 1u);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (base + u * kLsThreads < hi) atomicAdd(&s_hist[bucket_of(q, code[u])], 1u);
   }
   if (FROM_POINTS && __syncthreads_or(bad) && threadIdx.x == 0) raise_status(status, kStatusRange);
   __syncthreads();
   uint32_t* row = chunk_hist + (size_t)c * nb;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) row[b] = s_hist[b];
+  for (int b = threadIdx.x; b < nb; b += kLsThreads) row[b] = s_hist[b];
 }
 
 // --------------------------------------------------------------- offsets --
@@ -94,10 +169,11 @@ __global__ void __launch_bounds__(256)
 }
 
 // One block: bucket starts (exclusive scan of totals), overflow fraction and
-// the fallback decision.
+// the fallback decision (also taken when the model's tables do not match).
 __global__ void __launch_bounds__(1024)
     lsort_scan_kernel(const uint32_t* __restrict__ totals, int nb, int n, float threshold,
-                      uint32_t* __restrict__ starts, LsortStats* __restrict__ stats) {
+                      const char* __restrict__ blob, uint32_t* __restrict__ starts,
+                      LsortStats* __restrict__ stats) {
   __shared__ uint32_t warp_tot[32];
   __shared__ uint32_t total;
   __shared__ uint32_t s_over, s_max;
@@ -134,8 +210,12 @@ __global__ void __launch_bounds__(1024)
     stats->n = (uint32_t)n;
     const float frac = n > 0 ? (float)s_over / (float)n : 0.f;
     stats->overflow_frac = frac;
-    // Fallback when too many keys sit in oversized buckets (load imbalance).
-    if (frac > threshold) {
+    const LcdfHeader* h = reinterpret_cast<const LcdfHeader*>(blob);
+    const bool model_ok = h->magic == kLcdfMagic && h->version == kLcdfVersion &&
+                          h->n_buckets == nb;
+    // Fallback when too many keys sit in oversized buckets (load imbalance)
+    // or when the bucket tables belong to another bucket count.
+    if (frac > threshold || !model_ok) {
       stats->skip = 1u;
       stats->fallback = 1u;
     }
@@ -143,7 +223,7 @@ __global__ void __launch_bounds__(1024)
 }
 
 // --------------------------------------------------------------- scatter --
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kLsThreads, 2)
     lsort_scatter_kernel(const uint32_t* __restrict__ keys, int n, const char* __restrict__ blob,
                          LcdfLayout L, const uint32_t* __restrict__ chunk_off,
                          const uint32_t* __restrict__ starts, int nb, uint32_t* __restrict__ out,
@@ -151,212 +231,357 @@ __global__ void __launch_bounds__(256)
   if (stats->skip) return;
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
-  LcdfTables t = lcdf_load_tables(blob, L, sm + align_up(4 * (size_t)nb, 16));
   const int G = gridDim.x, c = blockIdx.x;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+  for (int b = threadIdx.x; b < nb; b += kLsThreads)
     cursor[b] = starts[b] + chunk_off[(size_t)c * nb + b];
-  __syncthreads();
+  const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
+                                     reinterpret_cast<uint16_t*>(cursor + 2 * nb));
   const int lo = (int)((long long)n * c / G), hi = (int)((long long)n * (c + 1) / G);
-  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    const uint32_t k = keys[i];
-    const uint32_t pos = atomicAdd(&cursor[min(lcdf_bucket(t, k), (uint32_t)(nb - 1))], 1u);
-    if (pos < (uint32_t)n) out[pos] = k;
+  for (int base = lo + threadIdx.x; base < hi; base += kLsUnroll * kLsThreads) {
+    uint32_t k[kLsUnroll];
+#pragma unroll
+    for (int u = 0; u < kLsUnroll; ++u) {
+      const int i = base + u * kLsThreads;
+      if (i < hi) k[u] = keys[i];
+    }
+#pragma unroll
+    for (int u = 0; u < kLsUnroll; ++u) {
+      if (base + u * kLsThreads < hi) {
+        const uint32_t pos = atomicAdd(&cursor[bucket_of(q, k[u])], 1u);
+        if (pos < (uint32_t)n) out[pos] = k[u];
+      }
+    }
   }
 }
 
 // ---------------------------------------------------------------- buckets --
-constexpr unsigned long long kLbAggB = 1ull << 62;
-constexpr unsigned long long kLbIncB = 2ull << 62;
-constexpr unsigned long long kLbFlagsB = 3ull << 62;
-
-__device__ uint32_t bucket_lookback(unsigned long long* lb, int tile, uint32_t agg,
-                                    uint32_t* status) {
-  const int lane = threadIdx.x & 31;
-  if (tile == 0) {
-    if (lane == 0) st_release_u64(lb, kLbIncB | agg);
-    return 0;
-  }
-  if (lane == 0) st_release_u64(lb + tile, kLbAggB | agg);
-  uint32_t ex = 0;
-  int pred = tile - 1;
-  uint32_t spins = 0;
-  while (true) {
-    const int p = pred - lane;
-    const unsigned long long w = p >= 0 ? ld_relaxed_u64(lb + p) : kLbIncB;
-    const unsigned long long f = w & kLbFlagsB;
-    const uint32_t inc_m = __ballot_sync(0xffffffffu, f == kLbIncB);
-    const uint32_t nr_m = __ballot_sync(0xffffffffu, f == 0);
-    const int first_inc = inc_m ? __ffs(inc_m) - 1 : 32;
-    const int first_nr = nr_m ? __ffs(nr_m) - 1 : 32;
-    if (first_nr < first_inc) {
-      ex += __reduce_add_sync(0xffffffffu, lane < first_nr ? (uint32_t)w : 0u);
-      pred -= first_nr;
-      if (++spins > kSpinLimit) {
-        if (lane == 0) raise_status(status, kStatusSpinTimeout);
-        break;
-      }
-      backoff(spins);
-      continue;
-    }
-    const int take = first_inc < 32 ? first_inc + 1 : 32;
-    ex += __reduce_add_sync(0xffffffffu, lane < take ? (uint32_t)w : 0u);
-    if (first_inc < 32) break;
-    pred -= 32;
-  }
-  if (lane == 0) st_release_u64(lb + tile, kLbIncB | (uint32_t)(ex + agg));
-  return ex;
-}
-
 struct BucketSmem {
-  uint32_t bitmap[kBmWords];  // 64 KiB; the bitonic path reuses it for keys
-  uint32_t warp_tot[32];
+  uint32_t buf[kBkWords];  // keys cache + bitmap or radix ping-pong, whole-region bitmap, or bitonic keys
+  uint16_t whist[kBkWarps][kRsBins];  // radix sort: per-warp digit counts, then offsets
+  uint32_t dstart[kRsBins];           // radix sort: first position of each digit
+  uint32_t red[2][kBkWarps];
+  uint32_t warp_base[32];
   uint32_t misc[8];
 };
 
-__global__ void __launch_bounds__(kBucketThreads)
-    lsort_bucket_kernel(const uint32_t* __restrict__ bkeys, const uint32_t* __restrict__ starts,
-                        int nb, uint32_t* __restrict__ out, int* __restrict__ d_unique,
-                        unsigned long long* __restrict__ lb, uint32_t* __restrict__ counter,
-                        LsortStats* __restrict__ stats, uint32_t* __restrict__ status) {
+// Stable LSD radix sort of a[0, cnt) (cnt <= kBkCache) on the low `bits`
+// bits of key - kmin, 8-bit digits, ping-pong between a and b. Warp w ranks
+// its contiguous kBkItems * 32 keys with ballot multi-split (peers = lanes
+// with the same digit), so ties keep input order. Returns the sorted array.
+__device__ uint32_t* bucket_radix_sort(uint32_t* a, uint32_t* b, int cnt, uint32_t kmin, int bits,
+                                       BucketSmem& S) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint32_t lt = lanemask_lt();
+  // every warp takes `items` rows of 32 keys (the last warps may be partial)
+  const int items = (cnt + kBkWarps * 32 - 1) / (kBkWarps * 32);
+  const int seg = items * 32;
+  for (int shift = 0; shift < bits; shift += kRsBits) {
+    for (int k = tid; k < kBkWarps * kRsBins / 2; k += kBkThreads)
+      reinterpret_cast<uint32_t*>(S.whist)[k] = 0;
+    __syncthreads();
+    uint32_t rk[kBkItems / 2];  // two 16-bit ranks per register; keys are re-read
+    uint16_t* wh = S.whist[wid];
+#pragma unroll
+    for (int it = 0; it < kBkItems; ++it) {
+      if (it >= items) break;
+      const int idx = wid * seg + it * 32 + lane;
+      const bool valid = idx < cnt;
+      const uint32_t key = valid ? a[idx] : 0u;
+      const uint32_t dg = ((key - kmin) >> shift) & (kRsBins - 1);
+      uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+      for (int bit = 0; bit < kRsBits; ++bit) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, (dg >> bit) & 1u);
+        peers &= ((dg >> bit) & 1u) ? bal : ~bal;
+      }
+      const uint32_t before = valid ? wh[dg] : 0u;
+      const uint32_t r = before + __popc(peers & lt);
+      if (it & 1) rk[it >> 1] |= r << 16;
+      else rk[it >> 1] = r;
+      __syncwarp();
+      if (valid && (peers & lt) == 0) wh[dg] = (uint16_t)(before + __popc(peers));
+      __syncwarp();
+    }
+    __syncthreads();
+    // per digit: exclusive offsets over warps, then digit starts over digits
+    uint32_t tot = 0;
+    if (tid < kRsBins) {
+#pragma unroll
+      for (int w = 0; w < kBkWarps; ++w) {
+        const uint32_t c = S.whist[w][tid];
+        S.whist[w][tid] = (uint16_t)tot;
+        tot += c;
+      }
+    }
+    const uint32_t start = block_exclusive_sum<kBkThreads>(tid < kRsBins ? tot : 0u, S.warp_base,
+                                                           &S.misc[5]);
+    if (tid < kRsBins) S.dstart[tid] = start;
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kBkItems; ++it) {
+      if (it >= items) break;
+      const int idx = wid * seg + it * 32 + lane;
+      if (idx < cnt) {
+        const uint32_t key = a[idx];
+        const uint32_t dg = ((key - kmin) >> shift) & (kRsBins - 1);
+        const uint32_t r = (rk[it >> 1] >> ((it & 1) * 16)) & 0xffffu;
+        b[S.dstart[dg] + S.whist[wid][dg] + r] = key;
+      }
+    }
+    __syncthreads();
+    uint32_t* t = a;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+// Bitmap words [seg0, seg1) of this warp: lanes take consecutive words.
+// Pass 0 returns the warp's popcount; pass 1 emits keys at base + rank, into
+// shared memory (stage) or global memory.
+__device__ __forceinline__ uint32_t bitmap_emit(const uint32_t* bm, int seg0, int seg1,
+                                                uint32_t kmin, bool emit, uint32_t base,
+                                                uint32_t* dst) {
+  const int lane = threadIdx.x & 31;
+  uint32_t run = 0;
+  for (int w0 = seg0; w0 < seg1; w0 += 32) {
+    const int w = w0 + lane;
+    uint32_t bits = w < seg1 ? bm[w] : 0u;
+    const uint32_t c = __popc(bits);
+    uint32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (emit) {
+      uint32_t pos = base + run + inc - c;
+      const uint32_t kw = kmin + ((uint32_t)w << 5);
+      while (bits) {
+        const int bit = __ffs(bits) - 1;
+        bits &= bits - 1;
+        dst[pos++] = kw + (uint32_t)bit;
+      }
+    }
+    run += __shfl_sync(0xffffffffu, inc, 31);
+  }
+  return run;
+}
+
+// Sorted keys a[seg0, seg1) of this warp (a[-1] read for run heads).
+__device__ __forceinline__ uint32_t heads_emit(const uint32_t* a, int seg0, int seg1, bool emit,
+                                               uint32_t base, uint32_t* dst) {
+  const int lane = threadIdx.x & 31;
+  uint32_t run = 0;
+  for (int i0 = seg0; i0 < seg1; i0 += 32) {
+    const int i = i0 + lane;
+    const bool head = i < seg1 && (i == 0 || a[i] != a[i - 1]);
+    const uint32_t m = __ballot_sync(0xffffffffu, head);
+    if (emit && head) dst[base + run + __popc(m & lanemask_lt())] = a[i];
+    run += __popc(m);
+  }
+  return run;
+}
+
+// One CTA per bucket: the bucket's sorted unique keys overwrite the front of
+// its own range of bkeys (its keys are in shared memory, or in the bitmap,
+// by then) and its unique count goes to ucount[b]; buckets never wait on one
+// another. A scan of the counts and a copy kernel then pack the runs.
+__global__ void __launch_bounds__(kBkThreads, 3)
+    lsort_bucket_kernel(uint32_t* __restrict__ bkeys, const uint32_t* __restrict__ starts,
+                        uint32_t* __restrict__ ucount, LsortStats* __restrict__ stats) {
   // `skip` is final before this kernel starts; `fallback` may still be set by
-  // a failing bucket, and every bucket must publish its count regardless.
+  // a failing bucket.
   if (stats->skip) return;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   BucketSmem& S = *reinterpret_cast<BucketSmem*>(sm_raw);
-  const int tid = threadIdx.x;
-  if (tid == 0) S.misc[0] = atomicAdd(counter, 1u);
-  __syncthreads();
-  const int b = (int)S.misc[0];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int b = blockIdx.x;
   const uint32_t lo = starts[b], hi = starts[b + 1];
   const int cnt = (int)(hi - lo);
-  // key span of the bucket
+  const bool cached = cnt <= kBkCache;
+  // keys -> cache, and the key span of the bucket
   uint32_t kmin = 0xffffffffu, kmax = 0;
-  for (int i = tid; i < cnt; i += kBucketThreads) {
+  for (int i = tid; i < cnt; i += kBkThreads) {
     const uint32_t k = bkeys[lo + i];
+    if (cached) S.buf[i] = k;
     kmin = min(kmin, k);
     kmax = max(kmax, k);
   }
   kmin = __reduce_min_sync(0xffffffffu, kmin);
   kmax = __reduce_max_sync(0xffffffffu, kmax);
-  if ((tid & 31) == 0) {
-    S.warp_tot[tid >> 5] = kmin;
+  if (lane == 0) {
+    S.red[0][wid] = kmin;
+    S.red[1][wid] = kmax;
   }
   __syncthreads();
-  if (tid < 32) {
-    uint32_t v = tid < kBucketThreads / 32 ? S.warp_tot[tid] : 0xffffffffu;
-    v = __reduce_min_sync(0xffffffffu, v);
-    if (tid == 0) S.misc[1] = v;
-  }
-  __syncthreads();
-  if ((tid & 31) == 0) S.warp_tot[tid >> 5] = kmax;
-  __syncthreads();
-  if (tid < 32) {
-    uint32_t v = tid < kBucketThreads / 32 ? S.warp_tot[tid] : 0u;
-    v = __reduce_max_sync(0xffffffffu, v);
-    if (tid == 0) S.misc[2] = v;
+  if (wid == 0) {
+    uint32_t a = lane < kBkWarps ? S.red[0][lane] : 0xffffffffu;
+    uint32_t z = lane < kBkWarps ? S.red[1][lane] : 0u;
+    a = __reduce_min_sync(0xffffffffu, a);
+    z = __reduce_max_sync(0xffffffffu, z);
+    if (lane == 0) {
+      S.misc[1] = a;
+      S.misc[2] = z;
+    }
   }
   __syncthreads();
   kmin = S.misc[1];
   kmax = S.misc[2];
-  const uint32_t span = cnt > 0 ? kmax - kmin + 1u : 0u;
+  const uint32_t span_m1 = cnt > 0 ? kmax - kmin : 0u;  // span - 1
 
-  uint32_t uniq = 0;
-  int path;  // 0 bitmap, 1 bitonic, 2 cannot
-  if (cnt == 0) path = 0;
-  else if (span <= (uint32_t)kBmBits) path = 0;
-  else if (cnt <= kCap) path = 1;
-  else path = 2;
-
-  if (path == 2) {
-    if (tid == 0) {
-      atomicOr(&stats->fallback, 1u);
-      atomicAdd(&stats->failed_buckets, 1u);
+  // 0: bitmap in the second half, keys cached in the first (output staged);
+  //    taken while the bitmap has at most 2 words per key (dense buckets)
+  // 1: bitmap over the whole region (keys re-read, output written directly)
+  // 2: sorted keys: radix sort of the cached keys (cnt <= kBkCache) or
+  //    bitonic sort of up to kCap keys over the whole region
+  // 3: neither fits
+  const uint32_t words_needed = (span_m1 >> 5) + 1u;
+  int path;
+  bool radix = false;
+  if (cnt == 0) {
+    path = 0;
+  } else if (cached) {
+    if (span_m1 < kBmSmall && words_needed <= max(2u * (uint32_t)cnt, 256u)) {
+      path = 0;
+    } else {
+      path = 2;
+      radix = true;
     }
-    // still publish a count so later buckets' look-backs end
+  } else if (span_m1 < kBmBig) {
+    path = 1;
+  } else if (cnt <= kCap) {
+    path = 2;
+  } else {
+    path = 3;
   }
+  if (tid == 0 && cnt > 0)
+    atomicAdd(path <= 1 ? &stats->bitmap_buckets
+                        : path == 3 ? &stats->failed_buckets
+                                    : radix ? &stats->radix_buckets : &stats->bitonic_buckets,
+              1u);
 
-  const int words = path == 0 ? (int)((span + 31) >> 5) : 0;
-  if (path == 0 && cnt > 0) {
-    for (int w = tid; w < words; w += kBucketThreads) S.bitmap[w] = 0;
+  uint32_t* bm = path == 0 ? S.buf + kBkCache : S.buf;
+  uint32_t* sorted = S.buf;
+  const int words = (path <= 1 && cnt > 0) ? (int)words_needed : 0;
+  int n_items = 0;  // bitmap words or sorted keys walked by the count/emit passes
+  if (path <= 1) {
+    for (int w = tid; w < words; w += kBkThreads) bm[w] = 0;
     __syncthreads();
-    for (int i = tid; i < cnt; i += kBucketThreads) {
-      const uint32_t r = bkeys[lo + i] - kmin;
-      atomicOr(&S.bitmap[r >> 5], 1u << (r & 31));
+    if (path == 0) {
+      for (int i = tid; i < cnt; i += kBkThreads) {
+        const uint32_t r = S.buf[i] - kmin;
+        atomicOr(&bm[r >> 5], 1u << (r & 31));
+      }
+    } else {
+      for (int i = tid; i < cnt; i += kBkThreads) {
+        const uint32_t r = bkeys[lo + i] - kmin;
+        atomicOr(&bm[r >> 5], 1u << (r & 31));
+      }
     }
     __syncthreads();
-  } else if (path == 1) {
-    // bitonic sort of cnt keys padded to a power of two with 0xffffffff
+    n_items = words;
+  } else if (path == 2 && radix) {
+    const int bits = 32 - __clz(span_m1);
+    sorted = bucket_radix_sort(S.buf, S.buf + kBkCache, cnt, kmin, bits, S);
+    n_items = cnt;
+  } else if (path == 2) {
     int m = 1;
     while (m < cnt) m <<= 1;
-    for (int i = tid; i < m; i += kBucketThreads) S.bitmap[i] = i < cnt ? bkeys[lo + i] : 0xffffffffu;
+    for (int i = tid; i < m; i += kBkThreads) S.buf[i] = i < cnt ? bkeys[lo + i] : 0xffffffffu;
     __syncthreads();
+    // bitonic network over m keys; each thread takes m / 2 / kBkThreads pairs
     for (int k = 2; k <= m; k <<= 1) {
       for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = tid; i < m; i += kBucketThreads) {
-          const int p = i ^ j;
-          if (p > i) {
-            const uint32_t a = S.bitmap[i], c = S.bitmap[p];
-            const bool up = (i & k) == 0;
-            if ((a > c) == up) {
-              S.bitmap[i] = c;
-              S.bitmap[p] = a;
-            }
+        for (int p = tid; p < (m >> 1); p += kBkThreads) {
+          const int i = ((p & ~(j - 1)) << 1) | (p & (j - 1));
+          const uint32_t a = S.buf[i], c = S.buf[i + j];
+          if ((a > c) == ((i & k) == 0)) {
+            S.buf[i] = c;
+            S.buf[i + j] = a;
           }
         }
         __syncthreads();
       }
     }
+    n_items = cnt;
+  } else if (tid == 0) {
+    atomicOr(&stats->fallback, 1u);
   }
 
-  // Count unique keys: bitmap popcounts, or run heads of the sorted keys.
-  constexpr int kPer = kBmWords / kBucketThreads;  // words per thread (contiguous)
-  uint32_t mine = 0;
-  if (path == 0) {
-    const int w0 = tid * kPer;
-#pragma unroll 4
-    for (int q = 0; q < kPer; ++q)
-      if (w0 + q < words) mine += __popc(S.bitmap[w0 + q]);
-  } else if (path == 1) {
-    const int per = (cnt + kBucketThreads - 1) / kBucketThreads;
-    const int i0 = tid * per;
-    for (int q = 0; q < per; ++q) {
-      const int i = i0 + q;
-      if (i < cnt && (i == 0 || S.bitmap[i] != S.bitmap[i - 1])) ++mine;
+  // Warp segments of the walked items: count, scan over warps, emit.
+  const int per_warp = ((n_items + kBkWarps - 1) / kBkWarps + 31) & ~31;
+  const int seg0 = min(wid * per_warp, n_items), seg1 = min(seg0 + per_warp, n_items);
+  uint32_t wcount = 0;
+  if (path <= 1) wcount = bitmap_emit(bm, seg0, seg1, kmin, false, 0, nullptr);
+  else if (path == 2) wcount = heads_emit(sorted, seg0, seg1, false, 0, nullptr);
+  if (lane == 0) S.warp_base[wid] = wcount;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t x = lane < kBkWarps ? S.warp_base[lane] : 0u;
+    uint32_t inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
     }
-  }
-  uint32_t total_u;
-  const uint32_t my_off = block_exclusive_sum<kBucketThreads>(mine, S.warp_tot, &S.misc[3]);
-  total_u = S.misc[3];
-  uniq = path == 2 ? 0u : total_u;
-  if (tid < 32) {
-    const uint32_t e = bucket_lookback(lb, b, uniq, status);
-    if (tid == 0) S.misc[4] = e;
+    if (lane < kBkWarps) S.warp_base[lane] = inc - x;
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    if (lane == 0) S.misc[3] = path == 3 ? 0u : total;
   }
   __syncthreads();
-  const uint32_t ex = S.misc[4];
-  if (path == 0 && cnt > 0) {
-    uint32_t o = ex + my_off;
-    const int w0 = tid * kPer;
-    for (int q = 0; q < kPer; ++q) {
-      const int w = w0 + q;
-      if (w >= words) break;
-      uint32_t bits = S.bitmap[w];
-      while (bits) {
-        const int bit = __ffs(bits) - 1;
-        bits &= bits - 1;
-        out[o++] = kmin + ((uint32_t)w << 5) + (uint32_t)bit;
-      }
-    }
+  const uint32_t uniq = S.misc[3];
+  const uint32_t wbase = S.warp_base[wid];
+  uint32_t* dst = bkeys + lo;
+  if (path == 0 && uniq > 0) {
+    // stage the bucket's unique keys over the key cache, then copy out coalesced
+    bitmap_emit(bm, seg0, seg1, kmin, true, wbase, S.buf);
+    __syncthreads();
+    for (uint32_t i = tid; i < uniq; i += kBkThreads) dst[i] = S.buf[i];
   } else if (path == 1) {
-    const int per = (cnt + kBucketThreads - 1) / kBucketThreads;
-    const int i0 = tid * per;
-    uint32_t o = ex + my_off;
-    for (int q = 0; q < per; ++q) {
-      const int i = i0 + q;
-      if (i < cnt && (i == 0 || S.bitmap[i] != S.bitmap[i - 1])) out[o++] = S.bitmap[i];
+    bitmap_emit(bm, seg0, seg1, kmin, true, wbase, dst);
+  } else if (path == 2) {
+    heads_emit(sorted, seg0, seg1, true, wbase, dst);
+  }
+  if (tid == 0) ucount[b] = uniq;
+}
+
+// One block: exclusive scan of the per-bucket unique counts; U to *d_unique.
+__global__ void __launch_bounds__(1024)
+    lsort_uscan_kernel(const uint32_t* __restrict__ ucount, int nb, uint32_t* __restrict__ uoff,
+                       int* __restrict__ d_unique, const LsortStats* __restrict__ stats) {
+  if (stats->fallback) return;  // final once the bucket kernel is done
+  __shared__ uint32_t warp_tot[32];
+  __shared__ uint32_t total;
+  const int per = (nb + 1023) / 1024;
+  uint32_t sum = 0;
+  for (int j = 0; j < per; ++j) {
+    const int b = threadIdx.x * per + j;
+    if (b < nb) sum += ucount[b];
+  }
+  uint32_t run = block_exclusive_sum<1024>(sum, warp_tot, &total);
+  for (int j = 0; j < per; ++j) {
+    const int b = threadIdx.x * per + j;
+    if (b < nb) {
+      uoff[b] = run;
+      run += ucount[b];
     }
   }
-  if (tid == 0 && b == nb - 1) *d_unique = (int)(ex + uniq);
+  if (threadIdx.x == 0) *d_unique = (int)total;
+}
+
+// One block per bucket: its unique run, from the front of its bkeys range to
+// its place in the output.
+__global__ void __launch_bounds__(256)
+    lsort_compact_kernel(const uint32_t* __restrict__ bkeys, const uint32_t* __restrict__ starts,
+                         const uint32_t* __restrict__ ucount, const uint32_t* __restrict__ uoff,
+                         uint32_t* __restrict__ out, const LsortStats* __restrict__ stats) {
+  if (stats->fallback) return;
+  const int b = blockIdx.x;
+  const uint32_t* src = bkeys + starts[b];
+  uint32_t* dst = out + uoff[b];
+  const int c = (int)ucount[b];
+  for (int i = threadIdx.x; i < c; i += 256) dst[i] = src[i];
 }
 
 // Gate for the fallback launches: 1 when the learned path gave up.
@@ -382,7 +607,7 @@ LsortPlan lsort_plan(int n, int nb, int max_segments) {
   // zeroed each run:
   p.stats_off = take(sizeof(LsortStats));
   p.counter_off = take(64);
-  p.lookback_off = take(8 * (size_t)(nb + 1));
+  p.lookback_off = 0;  // unused: buckets publish counts, a scan packs them
   p.sort_ctrl_off = take(p.fallback_sort.bytes);
   p.uniq_ctrl_off = take(p.fallback_unique.bytes);
   p.zero_bytes = o;
@@ -390,14 +615,12 @@ LsortPlan lsort_plan(int n, int nb, int max_segments) {
   p.hist_off = take(4 * (size_t)p.chunks * nb);
   p.totals_off = take(4 * (size_t)nb);
   p.starts_off = take(4 * (size_t)(nb + 1));
+  p.ucount_off = take(4 * (size_t)nb);
+  p.uoff_off = take(4 * (size_t)nb);
   p.bkeys_off = take(4 * (size_t)(n > 0 ? n : 1));
   p.alt_off = take(4 * (size_t)(n > 0 ? n : 1));
   p.bytes = o;
   return p;
-}
-
-size_t lsort_hist_smem(int nb, int max_segments) {
-  return align_up(4 * (size_t)nb, 16) + lcdf_tables_smem(max_segments);
 }
 
 cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coord, float range,
@@ -408,10 +631,11 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   LsortStats* stats = reinterpret_cast<LsortStats*>(ws + p.stats_off);
   uint32_t* counter = reinterpret_cast<uint32_t*>(ws + p.counter_off);
   uint32_t* gate = counter + 1;
-  unsigned long long* lb = reinterpret_cast<unsigned long long*>(ws + p.lookback_off);
   uint32_t* hist = reinterpret_cast<uint32_t*>(ws + p.hist_off);
   uint32_t* totals = reinterpret_cast<uint32_t*>(ws + p.totals_off);
   uint32_t* starts = reinterpret_cast<uint32_t*>(ws + p.starts_off);
+  uint32_t* ucount = reinterpret_cast<uint32_t*>(ws + p.ucount_off);
+  uint32_t* uoff = reinterpret_cast<uint32_t*>(ws + p.uoff_off);
   uint32_t* bkeys = reinterpret_cast<uint32_t*>(ws + p.bkeys_off);
   uint32_t* alt = reinterpret_cast<uint32_t*>(ws + p.alt_off);
   const size_t hsm = lsort_hist_smem(p.nb, p.L.max_knots);
@@ -432,20 +656,22 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   if (e != cudaSuccess) return e;
   mark(rec, s);
   if (pts)
-    lsort_hist_kernel<true><<<p.chunks, 256, hsm, s>>>(pts, keys, n, min_coord, range, blob, p.L,
-                                                       hist, p.nb, status);
+    lsort_hist_kernel<true><<<p.chunks, kLsThreads, hsm, s>>>(pts, keys, n, min_coord, range,
+                                                              blob, p.L, hist, p.nb, status);
   else
-    lsort_hist_kernel<false><<<p.chunks, 256, hsm, s>>>(nullptr, keys, n, 0.f, 1.f, blob, p.L,
-                                                        hist, p.nb, status);
+    lsort_hist_kernel<false><<<p.chunks, kLsThreads, hsm, s>>>(nullptr, keys, n, 0.f, 1.f, blob,
+                                                               p.L, hist, p.nb, status);
   mark(rec, s);
   lsort_offsets_kernel<<<(p.nb + 31) / 32, 256, 0, s>>>(hist, p.chunks, p.nb, totals);
-  lsort_scan_kernel<<<1, 1024, 0, s>>>(totals, p.nb, n, threshold, starts, stats);
+  lsort_scan_kernel<<<1, 1024, 0, s>>>(totals, p.nb, n, threshold, blob, starts, stats);
   mark(rec, s);
-  lsort_scatter_kernel<<<p.chunks, 256, hsm, s>>>(keys, n, blob, p.L, hist, starts, p.nb, bkeys,
-                                                  stats);
+  lsort_scatter_kernel<<<p.chunks, kLsThreads, hsm, s>>>(keys, n, blob, p.L, hist, starts, p.nb,
+                                                         bkeys, stats);
   mark(rec, s);
-  lsort_bucket_kernel<<<p.nb, kBucketThreads, sizeof(BucketSmem), s>>>(
-      bkeys, starts, p.nb, out, d_unique, lb, counter, stats, status);
+  lsort_bucket_kernel<<<p.nb, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, starts, ucount, stats);
+  mark(rec, s);
+  lsort_uscan_kernel<<<1, 1024, 0, s>>>(ucount, p.nb, uoff, d_unique, stats);
+  lsort_compact_kernel<<<p.nb, 256, 0, s>>>(bkeys, starts, ucount, uoff, out, stats);
   mark(rec, s);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -583,17 +809,19 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
   int* d_max_slot = reinterpret_cast<int*>(w + L.misc_off + 8);
   uint32_t* keys = reinterpret_cast<uint32_t*>(w + L.keys_off);
   cudaError_t e = cudaMemsetAsync(w, 0, L.lsort_off, s);  // misc + scan control
+  // the tree's merge slots live in prefix_sum until the scan overwrites it
+  if (e == cudaSuccess) e = cudaMemsetAsync(out->prefix_sum, 0, sizeof(int32_t) * (size_t)n, s);
   if (e == cudaSuccess)
     e = launch_lsort(reinterpret_cast<const float4*>(points), keys, n, min_coord, range,
                      static_cast<const char*>(model), L.lp, w + L.lsort_off, overflow_threshold,
                      out->codes, d_unique, status, s, nullptr);
   if (e == cudaSuccess)
-    e = launch_radix_tree(n, d_unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
-                          out->tree.has_leaf_right, out->tree.left_child, out->tree.parent, s);
+    e = launch_radix_tree_bu(n, d_unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
+                             out->tree.has_leaf_right, out->tree.left_child, out->tree.parent,
+                             out->edge_count, reinterpret_cast<uint32_t*>(out->prefix_sum), s);
   if (e == cudaSuccess)
-    e = launch_edge_scan(kEdgeAndScan, n, d_unique, out->tree.prefix_n, out->tree.parent,
-                         out->edge_count, out->prefix_sum, d_max_slot, &L.scan, w + L.scan_off,
-                         status, s);
+    e = launch_edge_scan(kScanOnly, n, d_unique, nullptr, nullptr, out->edge_count,
+                         out->prefix_sum, d_max_slot, &L.scan, w + L.scan_off, status, s);
   if (e == cudaSuccess && out->nodes_capacity > 0) {
     OctArgs a{};
     a.nodes = out->nodes;

@@ -14,8 +14,12 @@ struct LsortStats {
   uint32_t n;
   float overflow_frac;      // overflow_keys / n
   uint32_t skip;            // set before the scatter when overflow_frac > threshold
-  uint32_t pad;
+  uint32_t bitmap_buckets;  // buckets sorted through a shared-memory bitmap
+  uint32_t radix_buckets;   // ... through the shared-memory radix sort
+  uint32_t bitonic_buckets; // ... through the bitonic sort
+  uint32_t pad[2];
 };
+static_assert(sizeof(LsortStats) == 48, "LsortStats is 12 words");
 
 struct LsortPlan {
   int n, nb, chunks;
@@ -23,7 +27,7 @@ struct LsortPlan {
   SortPlan fallback_sort;
   ScanPlan fallback_unique;
   size_t stats_off, counter_off, lookback_off, sort_ctrl_off, uniq_ctrl_off, zero_bytes;
-  size_t hist_off, totals_off, starts_off, bkeys_off, alt_off, bytes;
+  size_t hist_off, totals_off, starts_off, ucount_off, uoff_off, bkeys_off, alt_off, bytes;
 };
 
 LsortPlan lsort_plan(int n, int nb, int max_segments);

@@ -17,8 +17,9 @@ from . import _lib
 
 HEADER = struct.Struct("<IIiiiiffi")
 MAGIC = 0x4643444C
-VERSION = 1
-PART_NAMES = ("x", "theta", "adam_m", "adam_v", "y", "grad", "yq", "slope", "lut", "total")
+VERSION = 2
+PART_NAMES = ("x", "theta", "adam_m", "adam_v", "y", "grad", "yq", "slope", "lut", "bounds", "blut",
+              "total")
 
 
 def _stream():
@@ -29,7 +30,7 @@ class LearnedCDF:
     def __init__(self, max_segments: int = 1024, device="cuda"):
         self.lib = _lib.load()
         self.max_segments = int(max_segments)
-        offs = (C.c_size_t * 10)()
+        offs = (C.c_size_t * len(PART_NAMES))()
         _lib.check(self.lib.oct_lcdf_layout(self.max_segments, offs), "oct_lcdf_layout")
         self.offsets = dict(zip(PART_NAMES, [int(o) for o in offs]))
         self.device = torch.device(device)
@@ -97,7 +98,9 @@ class LearnedCDF:
                     theta=self.part("theta", np.float32, k),
                     yq=self.part("yq", np.uint32, k + 1).astype(np.int64),
                     slope=self.part("slope", np.uint64, k),
-                    n_buckets=h["n_buckets"])
+                    n_buckets=h["n_buckets"],
+                    bounds=self.part("bounds", np.uint32, max(h["n_buckets"], 0) + 1).astype(np.int64),
+                    blut=self.part("blut", np.uint16, (1 << 14) + 1).astype(np.int64))
 
     # -------------------------------------------------------- persistence --
     def state_dict(self) -> dict:

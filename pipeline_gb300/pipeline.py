@@ -131,7 +131,8 @@ class OctreeBuilder:
 
 
 LSORT_STATS = ("fallback", "failed_buckets", "overflow_keys", "max_bucket", "n", "overflow_frac",
-               "skip", "pad")
+               "skip", "bitmap_buckets", "radix_buckets", "bitonic_buckets")
+LSORT_STATS_WORDS = 12
 
 
 def decode_lsort_stats(t: torch.Tensor) -> dict:
@@ -151,7 +152,7 @@ def lsort_unique(keys: torch.Tensor, model, n_buckets: int | None = None,
     ws = torch.empty(max(ws_bytes, 256), dtype=torch.uint8, device=keys.device)
     out = torch.empty(max(n, 1), dtype=torch.int32, device=keys.device)
     d_u = torch.zeros(1, dtype=torch.int32, device=keys.device)
-    stats = torch.zeros(8, dtype=torch.int32, device=keys.device)
+    stats = torch.zeros(LSORT_STATS_WORDS, dtype=torch.int32, device=keys.device)
     s = torch.cuda.current_stream(keys.device)
     rc = lib.oct_lsort_unique(C.c_void_p(keys.data_ptr()), n, C.c_void_p(model.blob.data_ptr()),
                               model.max_segments, nb, float(overflow_threshold),
@@ -175,7 +176,7 @@ class LearnedOctreeBuilder(OctreeBuilder):
         ws = self.lib.oct_build_learned_workspace_bytes(self.n_max, self.cap, self.nb,
                                                         model.max_segments)
         self.workspace = torch.empty(max(ws, 256), dtype=torch.uint8, device=self.device)
-        self.stats = torch.zeros(8, dtype=torch.int32, device=self.device)
+        self.stats = torch.zeros(LSORT_STATS_WORDS, dtype=torch.int32, device=self.device)
 
     def build(self, points: torch.Tensor, min_coord: float, rng: float, n: int | None = None,
               stream: torch.cuda.Stream | None = None) -> None:

@@ -114,6 +114,30 @@ def test_buckets_exact_and_monotone():
     assert got.min() >= 0 and got.max() <= 1023
 
 
+def test_bucket_boundaries_match_reference():
+    """The boundary table the bucketed sort searches: bounds[b] is the smallest
+    key whose bucket is >= b, blut[p] the bucket of key p << 16 (CPU reference
+    buckets on the same fixed-point tables)."""
+    keys = np.sort(clustered_keys(80_000))
+    nb = 1024
+    m = model_on(keys, segments=256, steps=30, nb=nb)
+    t = m.tables()
+    bounds, blut = t["bounds"], t["blut"]
+    assert bounds[0] == 0 and bounds[nb] == 1 << 30
+    assert np.all(np.diff(bounds) >= 0)
+    inner = bounds[1:nb]
+    reach = inner < (1 << 30)
+    at = LR.buckets(inner[reach].astype(np.uint32), t["x"], t["yq"], t["slope"], nb)
+    assert np.all(at >= np.arange(1, nb)[reach])
+    before = LR.buckets((inner[reach] - 1).astype(np.uint32), t["x"], t["yq"], t["slope"], nb)
+    assert np.all(before < np.arange(1, nb)[reach])
+    top = LR.buckets(np.array([(1 << 30) - 1], np.uint32), t["x"], t["yq"], t["slope"], nb)[0]
+    assert np.all(np.arange(1, nb)[~reach] > top)
+    cells = np.minimum(np.arange((1 << 14) + 1, dtype=np.int64) << 16, (1 << 30) - 1)
+    want = LR.buckets(cells.astype(np.uint32), t["x"], t["yq"], t["slope"], nb)
+    assert np.array_equal(blut, want)
+
+
 def test_state_dict_round_trip():
     from pipeline_gb300.learned import LearnedCDF
 

@@ -109,6 +109,35 @@ def test_learned_build_matches_oracle(kind):
     assert b.lsort_stats()["fallback"] == 0
 
 
+@pytest.mark.parametrize("form", ["bitmap", "radix", "bitonic", "wide_bitmap"])
+def test_each_bucket_form_exact(form):
+    """Inputs chosen so the buckets take one shared-memory form: dense keys
+    (bitmap), sparse keys in small buckets (radix sort), sparse keys in
+    buckets of 8K-16K keys (bitonic), dense buckets of more than 8K keys
+    (whole-region bitmap). Duplicates included; result = np.unique."""
+    from pipeline_gb300.pipeline import lsort_unique
+
+    rng = np.random.default_rng(len(form))
+    if form == "bitmap":  # 256 keys per bucket over spans of ~1K keys
+        keys = rng.integers(0, 1 << 22, 1 << 20).astype(np.uint32)
+        m, want = fitted(keys, n_buckets=4096), "bitmap_buckets"
+    elif form == "radix":  # 256 keys per bucket over spans of 2^18
+        keys = rng.integers(0, 1 << 30, 1 << 20).astype(np.uint32)
+        m, want = no_model(4096), "radix_buckets"
+    elif form == "bitonic":  # ~12K keys per bucket over spans of 2^22
+        keys = rng.integers(0, 1 << 30, 12_000 * 256).astype(np.uint32)
+        m, want = no_model(256), "bitonic_buckets"
+    else:  # ~12K keys per bucket over spans of ~8K
+        keys = rng.integers(0, 1 << 21, 12_000 * 256).astype(np.uint32)
+        m, want = fitted(keys, n_buckets=256), "bitmap_buckets"
+    n7 = len(keys[1::7])
+    keys[1::7] = keys[:n7]  # duplicates across the array
+    out, st = lsort_unique(dev_keys(keys), m, overflow_threshold=1.0)
+    assert out.cpu().numpy().view(np.uint32).tobytes() == np.unique(keys).tobytes()
+    assert st["fallback"] == 0 and st["failed_buckets"] == 0, st
+    assert st[want] >= 0.9 * m.n_buckets, st
+
+
 @pytest.mark.parametrize("cfg", [(10, 16, 16, 0), (10, 16, 16, 1), (10, 16, 24, 1), (8, 16, 16, 0),
                                  (8, 16, 24, 1)])
 def test_every_sort_config_sorts(cfg):
