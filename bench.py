@@ -55,8 +55,8 @@ WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 
 # point (its digit histograms are fused, so the sort reads no extra 4 B/key);
 # each 10-bit sort pass reads and writes 4 B per key; unique reads 4 B per key
 # and writes 4 B per unique key; the radix tree reads 4 B per code and writes
-# 11 B per node plus its 4 B edge count; the prefix sum reads and writes 4 B
-# per node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
+# 11 B per node; edge count + prefix sum read 1+4+1 B and write 4+4 B per
+# node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
 # leaf link (split over the emit and finalize launches).
 def algorithmic_bytes(n, u, b, m):
     leaves = b + 1
@@ -66,8 +66,8 @@ def algorithmic_bytes(n, u, b, m):
         "sort pass 1": 8 * n,
         "sort pass 2": 8 * n,
         "unique": 4 * n + 4 * u,
-        "radix tree+edge count": 4 * u + 15 * b,
-        "prefix sum": 8 * b,
+        "radix tree": 4 * u + 11 * b,
+        "edge count+prefix sum": 14 * b,
         "octree emit": 40 * b + 4 * leaves,
         "octree finalize": 60 * m,
     }

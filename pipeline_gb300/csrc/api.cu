@@ -339,8 +339,6 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
 
   mark(rec, s);
   OCT_TRY(cudaMemsetAsync(w, 0, L.ctrl_bytes, s), "build: clear");
-  // the tree's merge slots live in prefix_sum until the scan overwrites it
-  OCT_TRY(cudaMemsetAsync(out->prefix_sum, 0, sizeof(int32_t) * (size_t)n, s), "build: clear");
   mark(rec, s);
   OCT_TRY(launch_morton(reinterpret_cast<const float4*>(points), keys_a, n, min_coord, range,
                         &L.sort, w + L.sort_off, m.status, s),
@@ -352,15 +350,14 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
   OCT_TRY(launch_unique(sorted, out->codes, n, m.unique, &L.uniq, w + L.uniq_off, m.status, s),
           "build: unique");
   mark(rec, s);
-  OCT_TRY(launch_radix_tree_bu(n, m.unique, out->codes, out->tree.prefix_n,
-                               out->tree.has_leaf_left, out->tree.has_leaf_right,
-                               out->tree.left_child, out->tree.parent, out->edge_count,
-                               reinterpret_cast<uint32_t*>(out->prefix_sum), s),
-          "build: radix tree + edge count");
+  OCT_TRY(launch_radix_tree(n, m.unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
+                            out->tree.has_leaf_right, out->tree.left_child, out->tree.parent, s),
+          "build: radix tree");
   mark(rec, s);
-  OCT_TRY(launch_edge_scan(kScanOnly, n, m.unique, nullptr, nullptr, out->edge_count,
-                           out->prefix_sum, m.max_slot, &L.scan, w + L.scan_off, m.status, s),
-          "build: prefix sum");
+  OCT_TRY(launch_edge_scan(kEdgeAndScan, n, m.unique, out->tree.prefix_n, out->tree.parent,
+                           out->edge_count, out->prefix_sum, m.max_slot, &L.scan, w + L.scan_off,
+                           m.status, s),
+          "build: edge count + prefix sum");
   mark(rec, s);
   if (out->nodes_capacity > 0) {
     OctArgs a{};
@@ -400,7 +397,7 @@ int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range
 
 static const char* const kBuildSteps[] = {
     "start",        "clear",         "morton+histogram", "histogram scan", "sort pass 0",
-    "sort pass 1",  "sort pass 2",   "unique",  "radix tree+edge count",  "prefix sum",
+    "sort pass 1",  "sort pass 2",   "unique",           "radix tree",     "edge count+prefix sum",
     "octree zero",  "octree emit",   "octree finalize",  "publish counts"};
 
 int oct_build_step_count(void) { return (int)(sizeof(kBuildSteps) / sizeof(kBuildSteps[0])); }

@@ -105,13 +105,6 @@ cudaError_t launch_unique_gated(const uint32_t* src, uint32_t* dst, int n, int* 
 
 // ---- radix tree, edge count, prefix sum -----------------------------------
 // n_nodes from the host (n_host) or, when d_unique != nullptr, as *d_unique - 1.
-// Whole-build form: tree + edge counts bottom-up; zeroed_slots holds
-// radix_tree_bu_slot_bytes(n) zero bytes (one word per split).
-size_t radix_tree_bu_slot_bytes(int n);
-cudaError_t launch_radix_tree_bu(int n_host, const int* d_unique, const uint32_t* codes,
-                                 uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
-                                 int* parent, int* edge_count, uint32_t* zeroed_slots,
-                                 cudaStream_t s);
 cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* codes,
                               uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
                               int* parent, cudaStream_t s);

@@ -809,19 +809,17 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
   int* d_max_slot = reinterpret_cast<int*>(w + L.misc_off + 8);
   uint32_t* keys = reinterpret_cast<uint32_t*>(w + L.keys_off);
   cudaError_t e = cudaMemsetAsync(w, 0, L.lsort_off, s);  // misc + scan control
-  // the tree's merge slots live in prefix_sum until the scan overwrites it
-  if (e == cudaSuccess) e = cudaMemsetAsync(out->prefix_sum, 0, sizeof(int32_t) * (size_t)n, s);
   if (e == cudaSuccess)
     e = launch_lsort(reinterpret_cast<const float4*>(points), keys, n, min_coord, range,
                      static_cast<const char*>(model), L.lp, w + L.lsort_off, overflow_threshold,
                      out->codes, d_unique, status, s, nullptr);
   if (e == cudaSuccess)
-    e = launch_radix_tree_bu(n, d_unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
-                             out->tree.has_leaf_right, out->tree.left_child, out->tree.parent,
-                             out->edge_count, reinterpret_cast<uint32_t*>(out->prefix_sum), s);
+    e = launch_radix_tree(n, d_unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
+                          out->tree.has_leaf_right, out->tree.left_child, out->tree.parent, s);
   if (e == cudaSuccess)
-    e = launch_edge_scan(kScanOnly, n, d_unique, nullptr, nullptr, out->edge_count,
-                         out->prefix_sum, d_max_slot, &L.scan, w + L.scan_off, status, s);
+    e = launch_edge_scan(kEdgeAndScan, n, d_unique, out->tree.prefix_n, out->tree.parent,
+                         out->edge_count, out->prefix_sum, d_max_slot, &L.scan, w + L.scan_off,
+                         status, s);
   if (e == cudaSuccess && out->nodes_capacity > 0) {
     OctArgs a{};
     a.nodes = out->nodes;

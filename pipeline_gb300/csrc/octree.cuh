@@ -35,74 +35,117 @@ __device__ __forceinline__ void put_child(const OctTags& t, int slot, int which,
 
 // Every write radix node i makes (MakeOctNodes for i >= 1 when mode has
 // kOctMake, LinkLeafNodes when it has kOctLink), as tags.
+//
+// Loads are grouped by dependency so each round is issued at once: the node's
+// own entries; then its parent's count and parent link and the codes of its
+// leaf children; then the rest of the walk up to the first radix node with
+// octree nodes (usually none); then that node's octree offset. At most one
+// walk applies: MakeOctNodes walks from parent[i] when i has octree nodes,
+// LinkLeafNodes walks from i, i.e. from parent[i] when i has none.
 __device__ __forceinline__ void emit_node(int mode, int i, const OctArgs& a, const OctTags& t,
                                           const Sizes& z, uint32_t* status) {
-  const int L = a.prefix_n[i] / 3;
-  if ((mode & kOctMake) && i >= 1) {
-    // include/shared/oct.h:24-90
-    const int k = a.counts[i];
-    if (k > 0) {
-      const int base = a.offsets[i];
-      const uint32_t code = a.codes[i];
-      for (int j = 0; j < k - 1; ++j) {
-        const int level = L - j;
-        const uint32_t pre = code >> (30 - 3 * level);
-        const int which = (int)(pre & 7u);
-        const int up = base + j + 1;
-        put_child(t, up, which, (((uint32_t)i << 4) | (uint32_t)j) + 1u, z.n_oct, status);
-        if ((unsigned)up < (unsigned)z.n_oct) atomicOr(&t.mask[up], 1u << which);
-        if ((unsigned)(base + j) < (unsigned)z.n_oct) atomicMax(&t.owner[base + j], (uint32_t)i);
-      }
-      int rp = a.parent[i];
-      int counter = 0;
-      bool bad = (unsigned)rp >= (unsigned)z.n_brt;
-      while (!bad && a.counts[rp] == 0) {
-        rp = a.parent[rp];
-        bad = (unsigned)rp >= (unsigned)z.n_brt;
-        if (++counter > 30) break;
-      }
-      if (bad) {  // malformed parent[]: never read out of bounds
-        raise_status(status, kStatusWalkLimit);
-        rp = 0;
-      }
-      const int top = L - k + 1;
-      const int which = (int)((code >> (30 - 3 * top)) & 7u);
-      const int oct_parent = a.offsets[rp];
-      put_child(t, oct_parent, which, (((uint32_t)i << 4) | (uint32_t)(k - 1)) + 1u, z.n_oct,
-                status);
-      if ((unsigned)oct_parent < (unsigned)z.n_oct) atomicOr(&t.mask[oct_parent], 1u << which);
-      const int slot = base + k - 1;
-      if ((unsigned)slot < (unsigned)z.n_oct) atomicMax(&t.owner[slot], (uint32_t)i);
-      else raise_status(status, kStatusCapacity);
-    }
+  const int pn = a.prefix_n[i];
+  const int k = a.counts[i];
+  const int par = a.parent[i];
+  const bool make = (mode & kOctMake) && i >= 1 && k > 0;
+  const bool ll = (mode & kOctLink) && a.hll[i];
+  const bool lr = (mode & kOctLink) && a.hlr[i];
+  const bool link = ll || lr;
+  int base = 0, lc = 0;
+  uint32_t code = 0;
+  if (make) {
+    base = a.offsets[i];
+    code = a.codes[i];
   }
-  if (mode & kOctLink) {
-    // include/shared/oct.h:92-134, walk bounded at radix node 0.
-    const bool l = a.hll[i], r = a.hlr[i];
-    if (l || r) {
-      int rn = i, steps = 0;
-      while (a.counts[rn] == 0 && rn != 0) {
-        const int up = a.parent[rn];
-        if ((unsigned)up >= (unsigned)z.n_brt || ++steps > 64) {
-          raise_status(status, kStatusWalkLimit);
-          break;
-        }
-        rn = up;
-      }
-      const int dst = a.offsets[rn];
-      const uint32_t sh = (uint32_t)(30 - 3 * (L + 1)) & 31u;
-      int lc = a.left_child[i];
-      if ((unsigned)lc >= (unsigned)z.n_brt) {  // leaf index lc + 1 <= n_brt must hold
-        raise_status(status, kStatusWalkLimit);
-        return;
-      }
-      if (l)
-        put_child(t, dst, (int)((a.codes[lc] >> sh) & 7u), kLinkTag | ((uint32_t)i << 1),
-                  z.n_oct, status);
-      if (r)
-        put_child(t, dst, (int)((a.codes[lc + 1] >> sh) & 7u),
-                  kLinkTag | ((uint32_t)i << 1) | 1u, z.n_oct, status);
+  if (link) lc = a.left_child[i];
+  const int L = pn / 3;
+  // walk start: the parent (MakeOctNodes; LinkLeafNodes of a node without
+  // octree nodes other than 0) or i itself (LinkLeafNodes otherwise)
+  const bool walk_link = link && k == 0 && i != 0;
+  const bool walk = make || walk_link;
+  int wc = 0, wp = 0;
+  uint32_t cl = 0, cr = 0;
+  const bool lc_ok = (unsigned)lc < (unsigned)z.n_brt;  // leaf index lc + 1 <= n_brt
+  const bool par_ok = (unsigned)par < (unsigned)z.n_brt;
+  if (walk && par_ok) {
+    wc = a.counts[par];
+    wp = a.parent[par];
+  }
+  if (link && lc_ok) {
+    if (ll) cl = a.codes[lc];
+    if (lr) cr = a.codes[lc + 1];
+  }
+
+  if (make) {
+    // include/shared/oct.h:24-90
+    for (int j = 0; j < k - 1; ++j) {
+      const int level = L - j;
+      const uint32_t pre = code >> (30 - 3 * level);
+      const int which = (int)(pre & 7u);
+      const int up = base + j + 1;
+      put_child(t, up, which, (((uint32_t)i << 4) | (uint32_t)j) + 1u, z.n_oct, status);
+      if ((unsigned)up < (unsigned)z.n_oct) atomicOr(&t.mask[up], 1u << which);
+      if ((unsigned)(base + j) < (unsigned)z.n_oct) atomicMax(&t.owner[base + j], (uint32_t)i);
     }
+    int rp = par;
+    bool bad = !par_ok;
+    if (!bad && wc == 0) {
+      int counter = 0;
+      rp = wp;
+      bad = (unsigned)rp >= (unsigned)z.n_brt;
+      if (!(++counter > 30))
+        while (!bad && a.counts[rp] == 0) {
+          rp = a.parent[rp];
+          bad = (unsigned)rp >= (unsigned)z.n_brt;
+          if (++counter > 30) break;
+        }
+    }
+    if (bad) {  // malformed parent[]: never read out of bounds
+      raise_status(status, kStatusWalkLimit);
+      rp = 0;
+    }
+    const int top = L - k + 1;
+    const int which = (int)((code >> (30 - 3 * top)) & 7u);
+    const int oct_parent = a.offsets[rp];
+    put_child(t, oct_parent, which, (((uint32_t)i << 4) | (uint32_t)(k - 1)) + 1u, z.n_oct,
+              status);
+    if ((unsigned)oct_parent < (unsigned)z.n_oct) atomicOr(&t.mask[oct_parent], 1u << which);
+    const int slot = base + k - 1;
+    if ((unsigned)slot < (unsigned)z.n_oct) atomicMax(&t.owner[slot], (uint32_t)i);
+    else raise_status(status, kStatusCapacity);
+  }
+  if (link) {
+    // include/shared/oct.h:92-134, walk bounded at radix node 0.
+    int rn = i;
+    if (walk_link) {
+      int steps = 0;
+      if (!par_ok) {
+        raise_status(status, kStatusWalkLimit);
+      } else {
+        rn = par;
+        ++steps;
+        int cnt = wc, up = wp;
+        while (cnt == 0 && rn != 0) {
+          if ((unsigned)up >= (unsigned)z.n_brt || ++steps > 64) {
+            raise_status(status, kStatusWalkLimit);
+            break;
+          }
+          rn = up;
+          cnt = a.counts[rn];
+          up = a.parent[rn];
+        }
+      }
+    }
+    const int dst = a.offsets[rn];
+    const uint32_t sh = (uint32_t)(30 - 3 * (L + 1)) & 31u;
+    if (!lc_ok) {
+      raise_status(status, kStatusWalkLimit);
+      return;
+    }
+    if (ll) put_child(t, dst, (int)((cl >> sh) & 7u), kLinkTag | ((uint32_t)i << 1), z.n_oct, status);
+    if (lr)
+      put_child(t, dst, (int)((cr >> sh) & 7u), kLinkTag | ((uint32_t)i << 1) | 1u, z.n_oct,
+                status);
   }
 }
 
@@ -119,6 +162,25 @@ __device__ __forceinline__ void finalize_slot(bool fresh, int p, const OctArgs& 
   const uint4 ta = c4[2 * p], tb = c4[2 * p + 1];
   const uint32_t tags[8] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
   const oct_node* nd = a.nodes + p;
+  const uint32_t m = t.mask[p];
+  const uint32_t own = t.owner[p];
+  // Every table read below depends only on the tags: issue them all at once.
+  int base[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const uint32_t g = tags[c];
+    const int* src = (g & kLinkTag) ? a.left_child + ((g & ~kLinkTag) >> 1)
+                                    : a.offsets + ((g - 1u) >> 4);
+    base[c] = 0;
+    if (g != 0) base[c] = __ldg(src);
+  }
+  int own_off = 0, own_pn = 0;
+  uint32_t own_code = 0;
+  if (own != 0) {
+    own_off = __ldg(a.offsets + own);
+    own_pn = __ldg(a.prefix_n + own);
+    own_code = __ldg(a.codes + own);
+  }
   uint32_t link_bits = 0;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
@@ -127,25 +189,20 @@ __device__ __forceinline__ void finalize_slot(bool fresh, int p, const OctArgs& 
     if (g == 0) {
       v = fresh ? 0 : nd->children[c];
     } else if (g & kLinkTag) {
-      const int i = (int)((g & ~kLinkTag) >> 1);
-      v = a.left_child[i] + (int)(g & 1u);
+      v = base[c] + (int)(g & 1u);
       link_bits |= 1u << c;
     } else {
-      const uint32_t q = g - 1u;
-      v = a.offsets[q >> 4] + (int)(q & 15u);
+      v = base[c] + (int)((g - 1u) & 15u);
     }
     w[c] = v;
   }
-  const uint32_t m = t.mask[p];
-  const uint32_t own = t.owner[p];
   float4 corner;
   float cell;
   if (own != 0) {
-    const int i = (int)own;
-    const int j = p - a.offsets[i];
-    const int level = a.prefix_n[i] / 3 - j;
+    const int j = p - own_off;
+    const int level = own_pn / 3 - j;
     const int sh = 30 - 3 * level;
-    corner = decode_corner((a.codes[i] >> sh) << sh, a.min_coord, a.range);
+    corner = decode_corner((own_code >> sh) << sh, a.min_coord, a.range);
     cell = __fdiv_rn(a.range, (float)(1 << (level - root_level)));
   } else if (fresh && p == 0) {
     const int sh = 30 - 3 * root_level;

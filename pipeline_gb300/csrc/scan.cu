@@ -347,75 +347,6 @@ __global__ void __launch_bounds__(256)
     radix_node(i, n, gc, prefix_n, hll, hlr, left_child, parent);
 }
 
-// Bottom-up tree + edge counts. One thread per leaf, kBuThreads leaves per
-// CTA: merges of splits between two of the CTA's leaves use shared-memory
-// slots; arrivals at other splits (or whose sibling never arrives from inside
-// the CTA) continue with the zeroed global slot array after the barrier.
-// Nothing waits: a climb ends at its first-arrival slot.
-constexpr int kBuThreads = 512;
-
-__global__ void __launch_bounds__(kBuThreads, 3)
-    radix_tree_bu_kernel(int n_host, const int* __restrict__ d_unique,
-                         const uint32_t* __restrict__ codes, BuOut o,
-                         uint32_t* __restrict__ g_slot) {
-  __shared__ uint32_t s_code[kBuThreads + 2];  // codes[b0 - 1, b0 + kBuThreads]
-  __shared__ uint32_t s_slot[kBuThreads];      // splits b0 .. b0 + kBuThreads - 2
-  const int N = d_unique ? *d_unique : n_host + 1;  // leaves
-  const int b0 = blockIdx.x * kBuThreads;
-  if (N < 2 || b0 >= N) return;
-  const int b1 = min(b0 + kBuThreads, N);
-  const int t = threadIdx.x;
-  for (int k = t; k < kBuThreads + 2; k += kBuThreads) {
-    const int j = b0 - 1 + k;
-    s_code[k] = (j >= 0 && j < N) ? codes[j] : 0u;
-  }
-  s_slot[t] = 0;
-  __syncthreads();
-  const SmemCodes sc{s_code, b0 - 1};
-  int pend_p = -1;
-  uint32_t pend_v = 0;
-  if (b0 + t < b1) {
-    int l = b0 + t, r = l;
-    for (int guard = 0; guard < 64; ++guard) {
-      const bool left = bu_delta(sc, r, N) > bu_delta(sc, l - 1, N);
-      const int p = left ? r : l - 1;
-      const uint32_t mine = left ? (uint32_t)l : (uint32_t)r;
-      if (p < b0 || p > b1 - 2) {  // split shared with a neighbouring CTA
-        pend_p = p;
-        pend_v = mine;
-        break;
-      }
-      const uint32_t prev = atomicExch(&s_slot[p - b0], mine + 1u);
-      if (prev == 0) break;
-      s_slot[p - b0] = 0;  // both children seen; leftovers are re-posted below
-      const int L = left ? l : (int)prev - 1, R = left ? (int)prev - 1 : r;
-      if (bu_form(sc, N, L, R, p, o)) break;
-      l = L;
-      r = R;
-    }
-  }
-  __syncthreads();
-  const GlobalCodes gc{codes};
-  if (pend_p >= 0) bu_climb_global(gc, N, pend_p, pend_v, o, g_slot);
-  if (b0 + t <= b1 - 2) {
-    const uint32_t v = s_slot[t];
-    if (v != 0) bu_climb_global(gc, N, b0 + t, v - 1u, o, g_slot);
-  }
-}
-
-size_t radix_tree_bu_slot_bytes(int n) { return align_up(4 * (size_t)(n > 0 ? n : 1), 256); }
-
-cudaError_t launch_radix_tree_bu(int n_host, const int* d_unique, const uint32_t* codes,
-                                 uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
-                                 int* parent, int* edge_count, uint32_t* zeroed_slots,
-                                 cudaStream_t s) {
-  if (n_host <= 0) return cudaSuccess;
-  const int grid = (n_host + kBuThreads - 1) / kBuThreads;
-  const BuOut o{prefix_n, hll, hlr, left_child, parent, edge_count};
-  radix_tree_bu_kernel<<<grid, kBuThreads, 0, s>>>(n_host, d_unique, codes, o, zeroed_slots);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* codes,
                               uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
                               int* parent, cudaStream_t s) {

@@ -85,135 +85,4 @@ __device__ __forceinline__ void radix_node(int i, int n, const Codes& codes,
   if (!leaf_r && gamma + 1 < n) parent[gamma + 1] = i;
 }
 
-// --------------------------------------------------------------------------
-// Bottom-up construction of the same tree (stage 4) plus the edge counts of
-// stage 5, for the whole-build paths.
-//
-// Leaves are the U = N codes, radix nodes the N - 1 splits between adjacent
-// codes. A subtree over leaves [l, r] hangs below the split r (it is the left
-// child) when delta(r, r+1) > delta(l-1, l), else below the split l - 1 (the
-// right child); deltas past either end count as -1. Each leaf climbs: at its
-// parent split it leaves its far bound in a slot with an atomic exchange; the
-// first of the two children to arrive stops there, the second reads its
-// sibling's bound and forms the node [L, R] with split p. This builds the
-// unique binary radix tree over distinct sorted keys, which is the tree the
-// reference's per-node searches produce for every node i >= 1; the node's
-// index is R when it is a left child and L when it is a right child (the
-// numbering of those searches), so it writes prefixN = delta(L, R),
-// leftChild = p, the two leaf flags, parent[] of its internal children and
-// their edge counts prefixN(child)/3 - prefixN(node)/3.
-//
-// Node 0 is the reference's special root: it spans keys [0, n-1], not
-// [0, n]. When the true root splits at p < n-1 it makes the same split (only
-// hasLeafRight can differ); when p = n-1 ("short root") node 0 repeats node
-// n-1 = keys [0, n-1]. The thread that forms the true root writes node 0 that
-// way; parent[] then equals the reference's (whose short-root writes node n-1
-// wins, and whose unwritten entries are the zeros the true root writes).
-// --------------------------------------------------------------------------
-struct BuOut {
-  uint8_t* prefix_n;
-  uint8_t* hll;
-  uint8_t* hlr;
-  int* left_child;
-  int* parent;
-  int* ec;
-};
-
-struct SmemCodes {
-  const uint32_t* s;  // codes[base, base + size)
-  int base;
-  __device__ __forceinline__ uint32_t operator[](int j) const { return s[j - base]; }
-};
-
-// delta between leaves k and k + 1, -1 past either end (N leaves)
-template <class Codes>
-__device__ __forceinline__ int bu_delta(const Codes& c, int k, int N) {
-  return (k < 0 || k > N - 2) ? -1 : delta_u8(c[k], c[k + 1]);
-}
-
-// Node 0 from the true root (split p over leaves [0, N-1]).
-template <class Codes>
-__device__ __forceinline__ void bu_root(const Codes& c, int N, int p, const BuOut& o) {
-  const int n = N - 1;
-  o.parent[0] = 0;
-  o.ec[0] = 0;
-  const uint32_t c0 = c[0];
-  if (n == 1) {  // one node over keys {0, 0}: clz(0) taken as 32
-    o.prefix_n[0] = (uint8_t)delta_u8(c0, c0);
-    o.left_child[0] = 0;
-    o.hll[0] = 1;
-    o.hlr[0] = 0;
-    return;
-  }
-  const int pn0 = delta_u8(c0, c[n - 1]);
-  o.prefix_n[0] = (uint8_t)pn0;
-  if (p < n - 1) {
-    o.left_child[0] = p;
-    o.hll[0] = p == 0;
-    o.hlr[0] = p + 1 == n - 1;
-    if (p != 0) {
-      o.parent[p] = 0;
-      o.ec[p] = delta_u8(c0, c[p]) / 3 - pn0 / 3;
-    }
-    o.parent[p + 1] = 0;  // keys [p+1, n]: at least two
-    o.ec[p + 1] = delta_u8(c[p + 1], c[n]) / 3 - pn0 / 3;
-  } else {
-    // short root: node n-1 (keys [0, n-1]) was formed before its parent; its
-    // former fenced after writing leftChild[n-1], so fence and read it past L1
-    __threadfence();
-    const int g = (int)__ldcg(reinterpret_cast<const unsigned int*>(o.left_child + n - 1));
-    o.left_child[0] = g;
-    o.hll[0] = g == 0;
-    o.hlr[0] = g + 1 == n - 1;
-    o.parent[n - 1] = 0;
-    o.ec[n - 1] = 0;  // prefixN[n-1] == prefixN[0]
-  }
-}
-
-// Form node [L, R] with split p; true when it was the root (climb over).
-template <class Codes>
-__device__ __forceinline__ bool bu_form(const Codes& c, int N, int L, int R, int p,
-                                        const BuOut& o) {
-  if (L == 0 && R == N - 1) {
-    bu_root(c, N, p, o);
-    return true;
-  }
-  const int kidx = bu_delta(c, R, N) > bu_delta(c, L - 1, N) ? R : L;
-  const uint32_t cL = c[L], cR = c[R];
-  const int pn = delta_u8(cL, cR);
-  o.prefix_n[kidx] = (uint8_t)pn;
-  o.left_child[kidx] = p;
-  o.hll[kidx] = L == p;
-  o.hlr[kidx] = R == p + 1;
-  if (L != p) {
-    o.parent[p] = kidx;
-    o.ec[p] = delta_u8(cL, c[p]) / 3 - pn / 3;
-  }
-  if (R != p + 1) {
-    o.parent[p + 1] = kidx;
-    o.ec[p + 1] = delta_u8(c[p + 1], cR) / 3 - pn / 3;
-  }
-  if (L == 0 && R == N - 2) __threadfence();  // node n-1 of a short root: see bu_root
-  return false;
-}
-
-// Climb with global slots from an arrival at split p carrying bound `mine`
-// (the child's range is [mine, p] or [p + 1, mine]).
-template <class Codes>
-__device__ __forceinline__ void bu_climb_global(const Codes& c, int N, int p, uint32_t mine,
-                                                const BuOut& o, uint32_t* slot) {
-  for (int guard = 0; guard < 64; ++guard) {
-    const uint32_t prev = atomicExch(&slot[p], mine + 1u);
-    if (prev == 0) return;
-    const bool was_left = (int)mine <= p;
-    const int L = was_left ? (int)mine : (int)prev - 1;
-    const int R = was_left ? (int)prev - 1 : (int)mine;
-    if (L < 0 || R >= N || L > p || R <= p) return;  // never for a zeroed slot array
-    if (bu_form(c, N, L, R, p, o)) return;
-    const bool left = bu_delta(c, R, N) > bu_delta(c, L - 1, N);
-    p = left ? R : L - 1;
-    mine = left ? (uint32_t)L : (uint32_t)R;
-  }
-}
-
 }  // namespace octgb
