@@ -109,6 +109,16 @@ OCT_API const char* oct_last_error(void);
 /* ----------------------------------------------------------------------- */
 OCT_API void oct_init_random_vec4(oct_vec4* out, int n, float min_coord, float range, int seed);
 
+/* Stage 0 (device): the reference's device generator gpu::k_InitRandomVec4  */
+/* (include/cuda/kernels/00_init.cuh:7-8, kernels/cuda/00_init.cu:11-50) as  */
+/* its driver launches it (apps/gpu_demo/main.cu:168-175, one element per    */
+/* thread): element i seeds four states from (4i + k) * seed, takes one step */
+/* of the hybrid Tausworthe/LCG generator and maps 24 bits of z1^z2, z2^z3,  */
+/* z3^z4, z1^z4 to fma(u / 2^24, range, min) (x, y, z, w; w is random too).  */
+/* d_points: DEVICE pointer, 16-byte aligned. Asynchronous on `stream`.      */
+OCT_API int oct_init_random_vec4_device(oct_vec4* d_points, int n, float min_coord, float range,
+                                        int seed, oct_stream_t stream);
+
 /* ----------------------------------------------------------------------- */
 /* Stage 1: Morton encode. Replaces k_ComputeMortonCode                     */
 /* (include/kernels/01_morton.hpp:9-13; GPU kernels/cuda/01_morton.cu:8-19).*/
@@ -348,6 +358,29 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* plan, const void* d_tab
 /* Synchronous convenience: copies d_counts to the host after the stream
  * drains and maps the status word to OCT_ERR_DEVICE / OCT_ERR_CAPACITY. */
 OCT_API int oct_read_counts(const int32_t* d_counts, int32_t* h_counts, oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Octree consumers: Morton decode and the tree check.                      */
+/* oct_morton_decode: d_out[i] = morton32_to_xyz(codes[i]) (include/shared/ */
+/* morton.h:45-80): per axis (raw / 1024) * range + min in FP32 without      */
+/* contraction, w = 1. d_out 16-byte aligned.                                */
+/* oct_check_tree: checkTree (apps/cpu_demo/main.cpp:13-35) from node        */
+/* root_index with (root_prefix, root_code_len): child_node_mask bits        */
+/* descend to children[c] with prefix << 3 | c and code length + 3;          */
+/* child_leaf_mask bits compare codes[children[c]] >> (30 - length - 3) with  */
+/* that prefix. d_counts (4 x int64, device) = {nodes visited, leaf checks,   */
+/* mismatches, rejected}; rejected counts steps the reference would take out */
+/* of bounds (child index outside the arrays, code length past 30) and, on a */
+/* malformed tree, visits beyond n_nodes per level. No counterpart runs in    */
+/* the reference's drivers (the function is defined but not called).         */
+/* ----------------------------------------------------------------------- */
+OCT_API int oct_morton_decode(const uint32_t* codes, int n, float min_coord, float range,
+                              oct_vec4* d_out, oct_stream_t stream);
+OCT_API size_t oct_check_tree_workspace_bytes(int n_nodes);
+OCT_API int oct_check_tree(const oct_node* nodes, int n_nodes, const uint32_t* codes, int n_codes,
+                           uint32_t root_prefix, int root_code_len, int root_index,
+                           long long* d_counts, void* workspace, size_t workspace_bytes,
+                           oct_stream_t stream);
 
 #ifdef __cplusplus
 } /* extern "C" */

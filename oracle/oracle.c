@@ -127,6 +127,28 @@ void orc_init_random_vec4(float* out, int n, float min, float range, int seed) {
   }
 }
 
+/* The reference's device generator (kernels/cuda/00_init.cu:11-50) as its   */
+/* driver launches it (apps/gpu_demo/main.cu:168-175: ceil(n/768) blocks of   */
+/* 768 threads, so thread i makes element i): four 32-bit states seeded with  */
+/* (4i + k) * seed, one step of the hybrid Tausworthe/LCG generator (three    */
+/* Tausworthe steps + an LCG, GPU Gems 3 ch. 37), and the low 24 bits of      */
+/* z1^z2, z2^z3, z3^z4, z1^z4 mapped to min + u / 2^24 * range. nvcc's default */
+/* contraction makes that last step one fused multiply-add, so fmaf here.      */
+void orc_init_random_vec4_gpu(float* out, int n, float min, float range, int seed) {
+  const uint32_t sd = (uint32_t)seed;
+  for (int i = 0; i < n; ++i) {
+    const uint32_t b = (uint32_t)i << 2;
+    uint32_t z1 = b * sd, z2 = (b + 1u) * sd, z3 = (b + 2u) * sd, z4 = (b + 3u) * sd;
+    z1 = ((z1 & 4294967294u) << 12) ^ (((z1 << 13) ^ z1) >> 19);
+    z2 = ((z2 & 4294967288u) << 4) ^ (((z2 << 2) ^ z2) >> 25);
+    z3 = ((z3 & 4294967280u) << 17) ^ (((z3 << 3) ^ z3) >> 11);
+    z4 = z4 * 1664525u + 1013904223u;
+    const uint32_t v[4] = {z1 ^ z2, z2 ^ z3, z3 ^ z4, z1 ^ z4};
+    for (int k = 0; k < 4; ++k)
+      out[4 * (size_t)i + k] = fmaf((float)(v[k] & 0xFFFFFFu) / 16777216.0f, range, min);
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Stage 1: Morton encode (include/shared/morton.h:15-39,                     */
 /* kernels/01_morton.cpp:5-14). Quantise each axis as (v - min) / range *     */
@@ -174,6 +196,66 @@ static void decode_corner(float* out, uint32_t code, float min, float range) {
     out[a] = t + min;
   }
   out[3] = 1.0f;
+}
+
+/* morton32_to_xyz over an array (include/shared/morton.h:45-80). */
+void orc_morton_decode(const uint32_t* codes, long n, float min, float range, float* out) {
+  for (long i = 0; i < n; ++i) decode_corner(out + 4 * (size_t)i, codes[i], min, range);
+}
+
+/* checkTree (apps/cpu_demo/main.cpp:13-35) without recursion: from node      */
+/* oct_idx with (prefix, code_len), every child_node_mask bit continues at    */
+/* children[c] with (prefix << 3 | c, code_len + 3); every child_leaf_mask   */
+/* bit compares codes[children[c]] >> (30 - (code_len + 3)) with the child's  */
+/* prefix. Counts {nodes visited, leaf checks, mismatches, rejected}: a       */
+/* rejected step is a child index outside the arrays or a depth past 30 bits  */
+/* (where the reference would shift by a negative count or recurse forever).  */
+typedef struct {
+  int node;
+  uint32_t prefix;
+  int len;
+} orc_visit;
+
+void orc_check_tree(const orc_octnode* nodes, int n_nodes, const uint32_t* codes, int n_codes,
+                    uint32_t prefix, int code_len, int oct_idx, long long* counts) {
+  counts[0] = counts[1] = counts[2] = counts[3] = 0;
+  if (oct_idx < 0 || oct_idx >= n_nodes) {
+    counts[3] = 1;
+    return;
+  }
+  size_t cap = 1024, top = 0;
+  orc_visit* stack = (orc_visit*)malloc(cap * sizeof(orc_visit));
+  stack[top++] = (orc_visit){oct_idx, prefix, code_len};
+  while (top > 0) {
+    const orc_visit v = stack[--top];
+    const orc_octnode* nd = &nodes[v.node];
+    counts[0]++;
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t np = (v.prefix << 3) | (uint32_t)c;
+      if (nd->child_node_mask & (1 << c)) {
+        const int q = nd->children[c];
+        if (q < 0 || q >= n_nodes || v.len + 3 > MORTON_BITS) {
+          counts[3]++;
+        } else {
+          if (top == cap) {
+            cap *= 2;
+            stack = (orc_visit*)realloc(stack, cap * sizeof(orc_visit));
+          }
+          stack[top++] = (orc_visit){q, np, v.len + 3};
+        }
+      }
+      if (nd->child_leaf_mask & (1 << c)) {
+        const int leaf = nd->children[c];
+        if (leaf < 0 || leaf >= n_codes || v.len + 3 > MORTON_BITS) {
+          counts[3]++;
+        } else {
+          counts[1]++;
+          if ((codes[leaf] >> (MORTON_BITS - (v.len + 3))) != np) counts[2]++;
+        }
+      }
+    }
+  }
+  free(stack);
 }
 
 /* ------------------------------------------------------------------------ */

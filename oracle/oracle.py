@@ -85,6 +85,9 @@ def _bind(lib):
                                     P, P, P, P, P, C.c_int, P]),
         "orc_fnv1a64": (C.c_uint64, [P, C.c_size_t]),
         "orc_o7_walks": (C.c_int, [P, P, P, P, C.c_int]),
+        "orc_init_random_vec4_gpu": (None, [P, C.c_int, C.c_float, C.c_float, C.c_int]),
+        "orc_morton_decode": (None, [P, C.c_long, C.c_float, C.c_float, P]),
+        "orc_check_tree": (None, [P, C.c_int, P, C.c_int, C.c_uint32, C.c_int, C.c_int, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -146,6 +149,32 @@ def init_random_vec4(n: int, min_coord: float = 0.0, rng: float = 1024.0, seed: 
     out = np.empty((n, 4), np.float32)
     lib().orc_init_random_vec4(_p(out), n, min_coord, rng, seed)
     return out
+
+
+def init_random_vec4_gpu(n: int, min_coord: float = 0.0, rng: float = 1024.0, seed: int = 114514):
+    """The reference's device generator, element by element (see oracle.c)."""
+    out = np.empty((max(n, 0), 4), np.float32)
+    if n > 0:
+        lib().orc_init_random_vec4_gpu(_p(out), n, min_coord, rng, seed)
+    return out
+
+
+def morton_decode(codes: np.ndarray, min_coord: float, rng: float) -> np.ndarray:
+    c = np.ascontiguousarray(codes, np.uint32)
+    out = np.empty((len(c), 4), np.float32)
+    if len(c):
+        lib().orc_morton_decode(_p(c), len(c), min_coord, rng, _p(out))
+    return out
+
+
+def check_tree(nodes: np.ndarray, codes: np.ndarray, prefix: int, code_len: int, root: int = 0):
+    """checkTree counts: (visited, leaf_checks, mismatches, rejected)."""
+    nd = np.ascontiguousarray(nodes, OCTNODE_DTYPE)
+    c = np.ascontiguousarray(codes, np.uint32)
+    out = np.zeros(4, np.int64)
+    lib().orc_check_tree(_p(nd) if len(nd) else None, len(nd), _p(c) if len(c) else None, len(c),
+                         prefix, code_len, root, _p(out))
+    return tuple(int(v) for v in out)
 
 
 def morton(points: np.ndarray, min_coord: float, rng: float, threads: int = 1) -> np.ndarray:

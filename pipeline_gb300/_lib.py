@@ -94,6 +94,10 @@ SIGNATURES = {
     "oct_build_workspace_bytes": (Z, [I, I]),
     "oct_build_octree": (I, [P, I, F, F, C.POINTER(OctBuildOutputs), P, Z, P]),
     "oct_read_counts": (I, [P, P, P]),
+    "oct_init_random_vec4_device": (I, [P, I, F, F, I, P]),
+    "oct_morton_decode": (I, [P, I, F, F, P, P]),
+    "oct_check_tree_workspace_bytes": (Z, [I]),
+    "oct_check_tree": (I, [P, I, P, I, C.c_uint32, I, I, P, P, Z, P]),
     "oct_lcdf_layout": (I, [I, P]),
     "oct_lcdf_fit_workspace_bytes": (Z, [I]),
     "oct_lcdf_fit": (I, [P, I, I, I, F, I, P, I, P, Z, P]),

@@ -86,8 +86,9 @@ __global__ void __launch_bounds__(256)
     const float mn = B.mins[d.z], rg = B.ranges[d.z];
     for (int i = d.x + threadIdx.x; i < d.y; i += blockDim.x) {
       const float4 p = ld_stream_f4(pts + i);
-      bad |= !(in_range(p.x, mn, rg) && in_range(p.y, mn, rg) && in_range(p.z, mn, rg));
-      const uint32_t c = morton_code(p.x, p.y, p.z, mn, rg);
+      bool ok;
+      const uint32_t c = morton_code(p.x, p.y, p.z, mn, rg, ok);
+      bad |= !ok;
       keys[i] = c;
       for (int ps = 0; ps < passes; ++ps)
         atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);

@@ -114,22 +114,41 @@ __device__ __forceinline__ uint32_t compact3(uint32_t m) {
 
 // FP32 quantisation in the reference's operation order, each step rounded to
 // nearest with no contraction: (v - min) / range * 1024, truncated.
-__device__ __forceinline__ uint32_t quantise(float v, float min_coord, float range) {
-  const float q = __fmul_rn(__fdiv_rn(__fsub_rn(v, min_coord), range), 1024.0f);
+// One axis of include/shared/morton.h:15-22: (uint32)((v - min) / range * 1024)
+// with an IEEE single division, sets ok = false outside [min, min + range]
+// (or NaN), where the reference's float-to-uint cast is undefined.
+//
+// Only floor(RN(a / range) * 1024) is needed (a = v - min, the * 1024 is
+// exact), so t = RN(a * scale), scale = RN(1024 / range), stands in for it
+// whenever no integer lies within t * 2^-20 of t: t and RN(a / range) * 1024
+// are each within a relative 2^-23 of a * 1024 / range, so they are within
+// t * 2^-22.3 of each other and have the same floor. Otherwise (near a cell
+// boundary, t < 0, huge, NaN) the division itself decides.
+__device__ __forceinline__ uint32_t quantise(float v, float min_coord, float range, float scale,
+                                             bool& ok) {
+  const float a = __fsub_rn(v, min_coord);
+  const float t = __fmul_rn(a, scale);
+  const float k = floorf(t);
+  const float f = __fsub_rn(t, k);
+  const float m = __fmul_rn(t, 0x1p-20f);
+  if (t >= 0.0f && t < 0x1p22f && f > m && __fsub_rn(1.0f, f) > m) {
+    ok = ok && k < 1024.0f;
+    return (uint32_t)k;
+  }
+  const float q = __fmul_rn(__fdiv_rn(a, range), 1024.0f);
+  ok = ok && q >= 0.0f && q <= 1024.0f;
   return __float2uint_rz(q);
 }
 
-__device__ __forceinline__ bool in_range(float v, float min_coord, float range) {
-  // Outside [min, min + range] (or NaN) is undefined behaviour in the
-  // reference's float-to-uint cast; flag it.
-  const float q = __fmul_rn(__fdiv_rn(__fsub_rn(v, min_coord), range), 1024.0f);
-  return q >= 0.0f && q <= 1024.0f;
-}
-
+// 30-bit Morton code of a point (morton.h:15-39); ok as for quantise.
 __device__ __forceinline__ uint32_t morton_code(float x, float y, float z, float min_coord,
-                                                float range) {
-  return spread3(quantise(x, min_coord, range)) | (spread3(quantise(y, min_coord, range)) << 1) |
-         (spread3(quantise(z, min_coord, range)) << 2);
+                                                float range, bool& ok) {
+  const float scale = __fdiv_rn(1024.0f, range);
+  ok = true;
+  const uint32_t qx = quantise(x, min_coord, range, scale, ok);
+  const uint32_t qy = quantise(y, min_coord, range, scale, ok);
+  const uint32_t qz = quantise(z, min_coord, range, scale, ok);
+  return spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
 }
 
 // morton32_to_xyz: per axis (raw / 1024) * range + min, w = 1.

@@ -117,9 +117,9 @@ __global__ void __launch_bounds__(kLsThreads, 2)
       for (int u = 0; u < U; ++u) {
         const int i = base + u * kLsThreads;
         if (i < hi) {
-          bad |= !(in_range(p[u].x, min_coord, range) && in_range(p[u].y, min_coord, range) &&
-                   in_range(p[u].z, min_coord, range));
-          code[u] = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range);
+          bool ok;
+          code[u] = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range, ok);
+          bad |= !ok;
           keys[i] = code[u];
         }
       }

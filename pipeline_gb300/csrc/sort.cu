@@ -42,9 +42,9 @@ __global__ void __launch_bounds__(256)
     for (int u = 0; u < U; ++u) p[u] = ld_stream_f4(pts + i + u * stride);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      bad |= !(in_range(p[u].x, min_coord, range) && in_range(p[u].y, min_coord, range) &&
-               in_range(p[u].z, min_coord, range));
-      const uint32_t c = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range);
+      bool ok;
+      const uint32_t c = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range, ok);
+      bad |= !ok;
       keys[i + u * stride] = c;
       if (HIST)
         for (int ps = 0; ps < passes; ++ps)
@@ -53,9 +53,9 @@ __global__ void __launch_bounds__(256)
   }
   for (; i < n; i += stride) {
     const float4 p = ld_stream_f4(pts + i);
-    bad |= !(in_range(p.x, min_coord, range) && in_range(p.y, min_coord, range) &&
-             in_range(p.z, min_coord, range));
-    const uint32_t c = morton_code(p.x, p.y, p.z, min_coord, range);
+    bool ok;
+    const uint32_t c = morton_code(p.x, p.y, p.z, min_coord, range, ok);
+    bad |= !ok;
     keys[i] = c;
     if (HIST)
       for (int ps = 0; ps < passes; ++ps)

@@ -235,3 +235,38 @@ def k_LinkLeafNodes(nodes: torch.Tensor, node_offsets: torch.Tensor,
         _ptr(rt_prefixN, "rt_prefixN", torch.uint8, N), _ptr(rt_parents, "rt_parents", torch.int32, N),
         _ptr(rt_leftChild, "rt_leftChild", torch.int32, N), N, _ptr(ws, "workspace"), ws.numel(),
         _ptr(status, "status"), _stream()), "k_LinkLeafNodes")
+
+
+# ------------------------------------------------------------ consumers --
+def k_InitRandomVec4_device(points: torch.Tensor, n: int, min_coord: float, rng: float,
+                            seed: int) -> None:
+    """gpu::k_InitRandomVec4 (kernels/cuda/00_init.cu:27-50) into a CUDA
+    float32 [n, 4] tensor, on the current stream."""
+    p = _ptr(points, "points", torch.float32, 4 * n)
+    _lib.check(_lib.load().oct_init_random_vec4_device(p, n, min_coord, rng, seed, _stream()),
+               "oct_init_random_vec4_device")
+
+
+def morton_decode(codes: torch.Tensor, n: int, min_coord: float, rng: float) -> torch.Tensor:
+    """morton32_to_xyz (include/shared/morton.h:45-80) of n codes: [n, 4] float32."""
+    out = torch.empty((max(n, 1), 4), dtype=torch.float32, device=codes.device)
+    _lib.check(_lib.load().oct_morton_decode(_ptr(codes, "codes", None, n), n, min_coord, rng,
+                                             C.c_void_p(out.data_ptr()), _stream()),
+               "oct_morton_decode")
+    return out[:n]
+
+
+def check_tree(nodes: torch.Tensor, n_nodes: int, codes: torch.Tensor, n_codes: int,
+               root_prefix: int, root_code_len: int, root_index: int = 0) -> tuple:
+    """checkTree (apps/cpu_demo/main.cpp:13-35) on the GPU: (visited,
+    leaf checks, mismatches, rejected)."""
+    lib = _lib.load()
+    ws = _workspace(lib.oct_check_tree_workspace_bytes(n_nodes), nodes.device)
+    counts = torch.zeros(4, dtype=torch.int64, device=nodes.device)
+    _lib.check(lib.oct_check_tree(_ptr(nodes, "nodes", None, OCTNODE_WORDS * n_nodes), n_nodes,
+                                  _ptr(codes, "codes", None, n_codes), n_codes,
+                                  root_prefix & 0xFFFFFFFF,
+                                  root_code_len, root_index, C.c_void_p(counts.data_ptr()),
+                                  C.c_void_p(ws.data_ptr()), ws.numel(), _stream()),
+               "oct_check_tree")
+    return tuple(int(v) for v in counts.cpu().tolist())

@@ -98,3 +98,42 @@ def test_planted_mistake_is_caught(small_cases):
     bad = o["prefix_sum"].copy()
     bad[len(bad) // 2] += 1
     assert bad.tobytes() != case["prefix_sum"].tobytes()
+
+
+def test_device_generator_restatement_matches_numpy():
+    """The oracle's copy of the reference's device generator against an
+    independent numpy statement of the same integer steps (min = 0 and a
+    power-of-two range make the fused multiply-add exact in float64)."""
+    n, seed, rg = 3000, 114514, 1024.0
+    i = np.arange(n, dtype=np.uint64)
+    m32 = np.uint64(0xFFFFFFFF)
+    b = (i << np.uint64(2)) & m32
+    sd = np.uint64(seed & 0xFFFFFFFF)
+    z1, z2, z3, z4 = [((b + np.uint64(k)) * sd) & m32 for k in range(4)]
+    z1 = ((((z1 & np.uint64(4294967294)) << np.uint64(12)) & m32) ^ ((((z1 << np.uint64(13)) & m32) ^ z1) >> np.uint64(19)))
+    z2 = ((((z2 & np.uint64(4294967288)) << np.uint64(4)) & m32) ^ ((((z2 << np.uint64(2)) & m32) ^ z2) >> np.uint64(25)))
+    z3 = ((((z3 & np.uint64(4294967280)) << np.uint64(17)) & m32) ^ ((((z3 << np.uint64(3)) & m32) ^ z3) >> np.uint64(11)))
+    z4 = (z4 * np.uint64(1664525) + np.uint64(1013904223)) & m32
+    vals = [z1 ^ z2, z2 ^ z3, z3 ^ z4, z1 ^ z4]
+    want = np.stack([((v & np.uint64(0xFFFFFF)).astype(np.float64) / 16777216.0 * rg).astype(np.float32)
+                     for v in vals], 1)
+    got = O.init_random_vec4_gpu(n, 0.0, rg, seed)
+    assert got.tobytes() == want.tobytes()
+
+
+def test_check_tree_restatement_small():
+    """checkTree counts on a hand-made three-node octree."""
+    nodes = np.zeros(3, O.OCTNODE_DTYPE)
+    nodes[0]["child_node_mask"] = 0b101
+    nodes[0]["children"][0] = 1
+    nodes[0]["children"][2] = 2
+    nodes[1]["child_leaf_mask"] = 0b10   # child 1 of prefix 0: keys 0b000001...
+    nodes[1]["children"][1] = 0
+    nodes[2]["child_leaf_mask"] = 0b1    # child 0 of prefix 2: key 0b010000... expected
+    nodes[2]["children"][0] = 1
+    codes = np.array([1 << 24, 5 << 24], np.uint32)  # top 6 bits 000001 and 000101
+    # code 0 sits under prefix 0b000001 (match); code 1 under 0b000101, checked against 0b010000
+    assert O.check_tree(nodes, codes, 0, 0) == (3, 2, 1, 0)
+    nodes[2]["child_node_mask"] = 0b1000000
+    nodes[2]["children"][6] = 9  # out of range
+    assert O.check_tree(nodes, codes, 0, 0) == (3, 2, 1, 1)

@@ -71,6 +71,36 @@ def test_morton_nonzero_min_matches_oracle():
     assert u32(out).tobytes() == O.morton(pts, float(mn), float(rg)).tobytes()
 
 
+@pytest.mark.parametrize("mn,rg", [(0.0, 1024.0), (-37.3, 129.0000153), (1e-3, 3.0e-2),
+                                   (-5000.0, 9999.5), (0.25, 1.0)])
+def test_morton_cell_boundaries_match_oracle(mn, rg):
+    """Coordinates on and a few ulps either side of every cell boundary
+    min + k * range / 1024 (where the quotient's last bit decides the cell),
+    plus random ones: codes equal the oracle's IEEE-division encode."""
+    k = K()
+    mn, rg = np.float32(mn), np.float32(rg)
+    cells = np.arange(1025, dtype=np.float64)
+    base = (mn.astype(np.float64) + cells * rg.astype(np.float64) / 1024.0).astype(np.float32)
+    vals = [base]
+    for steps in (1, 2, 3):
+        up, down = base.copy(), base.copy()
+        for _ in range(steps):
+            up = np.nextafter(up, np.float32(np.inf))
+            down = np.nextafter(down, np.float32(-np.inf))
+        vals += [up, down]
+    v = np.concatenate(vals)
+    v = v[(v >= mn) & (v <= np.float32(mn + rg))]
+    rng = np.random.default_rng(int(abs(mn) * 1000) + 7)
+    n = 3 * len(v) + 200_000
+    pts = rng.uniform(float(mn), float(mn + rg), (n, 4)).astype(np.float32)
+    for axis in range(3):  # every boundary value on every axis
+        pts[axis * len(v):(axis + 1) * len(v), axis] = v
+    pts = np.clip(pts, mn, np.float32(mn + rg))
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    k.k_ComputeMortonCode(dev(pts), out, n, float(mn), float(rg))
+    assert u32(out).tobytes() == O.morton(pts, float(mn), float(rg)).tobytes()
+
+
 def test_morton_range_status():
     k = K()
     pts = np.zeros((1000, 4), np.float32)
