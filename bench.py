@@ -8,9 +8,11 @@ nodes and leaf links. One step = one whole build of that cloud.
   value  Mpoints/s with the points already resident in HBM, timed with CUDA
          events around each step (L2 flushed between steps; the 256 MiB input
          is also larger than L2);
-  e2e    the same metric through the C ABI call a user makes, with the step's
-         points copied host->device from pinned memory and the octree
-         (M OctNodes + counts) copied back inside the timed region;
+  e2e    the same metric through the public API (PipelinedBuilder over the
+         C ABI), each step copying its points host->device from pinned
+         memory and its octree (M OctNodes + counts) back; consecutive steps'
+         uploads, builds and downloads overlap on three streams
+         (serial_value: the same with no overlap);
   roofline  the dominant kernel's algorithmic bytes per launch over its
          average duration (CUDA events recorded by oct_build_octree_timed on
          the launching stream), against MEASURED_PEAKS.json's HBM copy rate;
@@ -363,7 +365,7 @@ def run_ours(args, rank, world, local_rank):
     base = None
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(pts_h)
-    launches_per_step = nsteps - 2  # every step but "start" and the memset "clear"
+    launches_per_step = build_launches()
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4),
@@ -381,9 +383,20 @@ def run_ours(args, rank, world, local_rank):
     return 0
 
 
+def build_launches() -> int:
+    """Kernel launches of one plain build under the active sort shape:
+    Morton, digit-base scan, per pass (tile histogram + tile scan +) pass,
+    unique, tree, edge count + scan, octree zero/emit/finalize, counts."""
+    from pipeline_gb300 import autotune
+
+    rb, _, _, scan = autotune.get_config()
+    passes = (30 + rb - 1) // rb
+    return 2 + passes * (3 if scan == 1 else 1) + 1 + 1 + 1 + 3 + 1
+
+
 def profile_only(args):
     """--warmup builds then exactly one more build of the workload: a short,
-    fixed launch sequence for ncu (12 kernel launches per build)."""
+    fixed launch sequence for ncu (build_launches() kernel launches per build)."""
     import torch
 
     from pipeline_gb300.pipeline import OctreeBuilder
