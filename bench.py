@@ -360,6 +360,10 @@ def run_ours(args, rank, world, local_rank):
         workloads["clustered_16m"] = clustered_workload(dev, flush, max(5, min(args.steps, 20)))
         torch.cuda.empty_cache()
         workloads["batched_512"] = batched_workload(dev, flush, max(5, min(args.steps, 20)))
+        torch.cuda.empty_cache()
+        workloads["sort_vs_cub"] = sort_bar_workload(dev, flush, max(5, min(args.steps, 20)), pts)
+        torch.cuda.empty_cache()
+        workloads["frames_224"] = frames_workload(dev, flush, max(5, min(args.steps, 20)))
     if rank != 0:
         return 0
     base = None
@@ -402,13 +406,28 @@ def profile_only(args):
     from pipeline_gb300.pipeline import OctreeBuilder
 
     n = int(args.points)
-    pts = torch.from_numpy(make_points(n)).cuda()
-    b = OctreeBuilder(n)
+    if args.profile_only == "learned":
+        # clustered cloud of n points, model fit on 2^18 of its Morton codes
+        from pipeline_gb300 import datasets
+        from pipeline_gb300.kernels import k_ComputeMortonCode
+        from pipeline_gb300.learned import LearnedCDF
+        from pipeline_gb300.pipeline import LearnedOctreeBuilder
+
+        pts = torch.from_numpy(datasets.clustered(n, seed=7)).cuda()
+        s_n = min(n, 1 << 18)
+        idx = torch.from_numpy(np.random.default_rng(1).integers(0, n, s_n)).cuda()
+        sk = torch.empty(s_n, dtype=torch.int32, device="cuda")
+        k_ComputeMortonCode(pts.index_select(0, idx).contiguous(), sk, s_n, MIN_COORD, RANGE)
+        model = LearnedCDF(max_segments=4096).fit(sk, n_segments=4096, steps=0, n_buckets=4096)
+        b = LearnedOctreeBuilder(n, model)
+    else:
+        pts = torch.from_numpy(make_points(n)).cuda()
+        b = OctreeBuilder(n)
     for _ in range(max(args.warmup, 0) + 1):
         b.build(pts, MIN_COORD, RANGE)
     torch.cuda.synchronize()
     c = b.counts()
-    print(f"profile build: U={c.n_unique} M={c.n_oct} status={c.status}")
+    print(f"profile build ({args.profile_only}): U={c.n_unique} M={c.n_oct} status={c.status}")
     return 0 if c.status == 0 else 1
 
 
@@ -521,18 +540,175 @@ def batched_workload(dev, flush, reps):
             "speedup": round(t_loop / t_batch, 3), "bit_exact_spot_check": bool(exact)}
 
 
+def frames_workload(dev, flush, reps):
+    """Scan-like frames (64 beams x 1,920 azimuth steps, ground plane + 40
+    boxes, 2 cm range noise; per-frame min/range): frames 32-255 built in one
+    batched launch sequence vs a per-frame loop, and per frame with a learned
+    CDF fit only on frames 0-31's Morton codes (model transfer across frames)
+    vs the plain per-frame build."""
+    import torch
+
+    from pipeline_gb300 import datasets
+    from pipeline_gb300.batch import BatchOctreeBuilder
+    from pipeline_gb300.kernels import k_ComputeMortonCode
+    from pipeline_gb300.learned import LearnedCDF
+    from pipeline_gb300.pipeline import LearnedOctreeBuilder, OctreeBuilder
+
+    frames, mins, ranges = datasets.scan_frames(256, seed=5)
+    fit_f, test_f = frames[:32], frames[32:]
+    sizes = [len(f) for f in test_f]
+    total = int(sum(sizes))
+    stream = torch.cuda.current_stream(dev)
+    # model: Morton codes of frames 0-31, each in its own quantisation frame
+    codes = []
+    for f, mn, rg in zip(fit_f, mins[:32], ranges[:32]):
+        p = torch.from_numpy(f).to(dev)
+        k = torch.empty(len(f), dtype=torch.int32, device=dev)
+        k_ComputeMortonCode(p, k, len(f), mn, rg)
+        codes.append(k)
+    sample = torch.cat(codes)
+    nb = 512
+    model = LearnedCDF(max_segments=1024).fit(sample, n_segments=1024, steps=100, lr=0.05,
+                                              n_buckets=nb)
+    pts = torch.from_numpy(np.concatenate(test_f, 0)).to(dev)
+    d_min = torch.tensor(mins[32:], dtype=torch.float32, device=dev)
+    d_rg = torch.tensor(ranges[32:], dtype=torch.float32, device=dev)
+    b = BatchOctreeBuilder(sizes, device=dev)
+    b.capture(pts, d_min, d_rg)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    views = [pts[offs[c]:offs[c + 1]] for c in range(len(sizes))]
+    single = OctreeBuilder(max(sizes), device=dev)
+    learned = LearnedOctreeBuilder(max(sizes), model, device=dev, n_buckets=nb)
+
+    def plain_loop():
+        for v, mn, rg in zip(views, mins[32:], ranges[32:]):
+            single.build(v, mn, rg)
+
+    def learned_loop():
+        for v, mn, rg in zip(views, mins[32:], ranges[32:]):
+            learned.build(v, mn, rg)
+
+    plain_loop()
+    learned_loop()
+    b.replay()
+    torch.cuda.synchronize(dev)
+    counts = b.cloud_counts()
+    exact, fallbacks, overflow = True, 0, []
+    for c in range(0, len(sizes), 16):
+        single.build(views[c], mins[32 + c], ranges[32 + c])
+        learned.build(views[c], mins[32 + c], ranges[32 + c])
+        r, lr_ = single.result(), learned.result()
+        st = learned.lsort_stats()
+        fallbacks += st["fallback"]
+        overflow.append(st["overflow_frac"])
+        exact &= r["oct_nodes"].tobytes() == b.cloud_result(c, counts)["oct_nodes"].tobytes()
+        exact &= r["oct_nodes"].tobytes() == lr_["oct_nodes"].tobytes()
+    t_batch = _time_events(b.replay, reps, stream, flush)
+    t_plain = _time_events(plain_loop, max(2, reps // 4), stream, flush)
+    t_learn = _time_events(learned_loop, max(2, reps // 4), stream, flush)
+    return {"workload": "frames: 224 scan-like frames (32-255) of 122,880 points, per-frame "
+                        "min/range; model fit on frames 0-31 (1024 segments, 512 buckets)",
+            "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
+            "per_frame_plain_mpts": round(total / t_plain / 1e3, 1),
+            "per_frame_learned_mpts": round(total / t_learn / 1e3, 1),
+            "batched_vs_loop": round(t_plain / t_batch, 3),
+            "learned_vs_plain_per_frame": round(t_plain / t_learn, 3),
+            "bit_exact_spot_check": bool(exact), "learned_fallbacks_in_spot_check": int(fallbacks),
+            "overflow_frac_max": round(max(overflow), 5), "fit_loss": model.header()["loss"]}
+
+
+def sort_bar_workload(dev, flush, reps, pts):
+    """The sort stage against CUB's DeviceRadixSort::SortKeys on the same
+    16,777,216 Morton codes (30-bit, device-resident, one sort per rep)."""
+    import torch
+
+    from pipeline_gb300 import _lib, build as native
+    from pipeline_gb300.kernels import _workspace, k_ComputeMortonCode
+
+    n = pts.shape[0]
+    src = torch.empty(n, dtype=torch.int32, device=dev)
+    k_ComputeMortonCode(pts, src, n, MIN_COORD, RANGE)
+    keys = torch.empty_like(src)
+    alt = torch.empty_like(src)
+    stream = torch.cuda.current_stream(dev)
+    lib = _lib.load()
+    ws = _workspace(lib.oct_sort_workspace_bytes(n, 30), dev)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def ours():
+        lib.oct_sort_keys(C.c_void_p(keys.data_ptr()), C.c_void_p(alt.data_ptr()), n, 30,
+                          C.c_void_p(ws.data_ptr()), ws.numel(), None, sp)
+
+    def timed(fn):
+        ts = []
+        for r in range(reps):
+            keys.copy_(src)
+            flush.fill_(r & 0xFF)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    t_ours = timed(ours)
+    ours()
+    torch.cuda.synchronize(dev)
+    want = torch.sort(src.view(torch.int32))[0]
+    ok_ours = torch.equal(keys, want)
+    out = {"workload": "sort stage: 16,777,216 30-bit Morton codes of the uniform cloud, "
+                       "device-resident", "ours_ms": round(t_ours, 4),
+           "ours_gkeys_s": round(n / t_ours / 1e6, 2), "ours_sorted": bool(ok_ours)}
+    path = native.build_bar()
+    if path is None:
+        out["cub"] = "unavailable: CUB did not build"
+        return out
+    bar = C.CDLL(path)
+    bar.bar_cub_sort_keys.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                      C.POINTER(C.c_size_t), C.c_void_p]
+    tb = C.c_size_t(0)
+    bar.bar_cub_sort_keys(None, None, n, 30, None, C.byref(tb), sp)
+    temp = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
+    cub_out = torch.empty_like(src)
+
+    def cub():
+        bar.bar_cub_sort_keys(C.c_void_p(keys.data_ptr()), C.c_void_p(cub_out.data_ptr()), n, 30,
+                              C.c_void_p(temp.data_ptr()), C.byref(tb), sp)
+
+    t_cub = timed(cub)
+    out.update({"cub_ms": round(t_cub, 4), "cub_gkeys_s": round(n / t_cub / 1e6, 2),
+                "cub_sorted": bool(torch.equal(cub_out, want)),
+                "ours_vs_cub": round(t_cub / t_ours, 3)})
+    return out
+
+
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_uniform_4m.txt")
+TRAFFIC_POINTS = 4194304
+TRAFFIC_KERNELS = {"morton+histogram": "morton_kernel<10, 1>", "unique": "unique_kernel",
+                   "radix tree": "radix_tree_kernel", "edge count+prefix sum": "edge_scan_kernel",
+                   "octree zero": "oct_zero_kernel", "octree emit": "oct_emit_kernel",
+                   "octree finalize": "oct_finalize_kernel"}
+
+
 def read_traffic(kernel_step: str, n: int):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/dram_traffic.txt: '<step name>|<bytes per launch>|<n>'),
-    scaled to n points; None when no capture covers it."""
-    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
-    if not os.path.exists(path):
+    """DRAM bytes (read + write) per launch of a kernel from the committed ncu
+    summary of the 4,194,304-point build, scaled to n points; None when the
+    summary does not cover it. At that size outputs may still sit in L2 when
+    a kernel ends, so this can fall below the algorithmic bytes."""
+    name = TRAFFIC_KERNELS.get(kernel_step)
+    if name is None or not os.path.exists(TRAFFIC_FILE):
         return None
-    with open(path) as f:
+    with open(TRAFFIC_FILE) as f:
         for ln in f:
-            parts = ln.strip().split("|")
-            if len(parts) == 3 and parts[0] == kernel_step:
-                return int(float(parts[1]) * n / float(parts[2]))
+            parts = ln.split()
+            if len(parts) >= 4 and ln.strip().startswith(name):
+                try:
+                    mb = float(parts[-3]) + float(parts[-2])
+                except ValueError:
+                    continue
+                return int(mb * 1e6 * n / TRAFFIC_POINTS)
     return None
 
 
@@ -545,7 +721,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the clustered (learned) and batched workloads")
-    ap.add_argument("--profile-only", action="store_true",
+    ap.add_argument("--profile-only", nargs="?", const="plain", choices=["plain", "learned"],
                     help="warm-up builds plus one build, no timing or output (for ncu captures)")
     ap.add_argument("--points", type=int, default=N_POINTS,
                     help="cloud size for --profile-only (smaller cases for multi-pass ncu captures)")

@@ -84,6 +84,8 @@ def scan_frames(n_frames: int = 256, seed: int = 5, beams: int = 64, steps: int 
     dirs = np.stack([ce * np.cos(azim)[None, :], ce * np.sin(azim)[None, :],
                      np.broadcast_to(se, (beams, steps))], -1).reshape(-1, 3)
     sensor_h = 1.8
+    with np.errstate(divide="ignore"):
+        inv32 = (1.0 / dirs).astype(np.float32)
     frames, mins, ranges = [], [], []
     for f in range(n_frames):
         # ground plane z = -sensor_h; boxes: centre (x, y), half sizes, height
@@ -94,16 +96,23 @@ def scan_frames(n_frames: int = 256, seed: int = 5, beams: int = 64, steps: int 
         dz = dirs[:, 2]
         ground = np.where(dz < -1e-6, -sensor_h / np.minimum(dz, -1e-6), np.inf)
         t = np.minimum(t, ground)
-        for bx, by, hx, hy, hz in boxes:
-            lo = np.array([bx - hx, by - hy, -sensor_h])
-            hi = np.array([bx + hx, by + hy, -sensor_h + hz])
-            with np.errstate(divide="ignore", invalid="ignore"):
-                t1 = (lo[None, :] - 0.0) / dirs
-                t2 = (hi[None, :] - 0.0) / dirs
-            tmin = np.nanmax(np.minimum(t1, t2), 1)
-            tmax = np.nanmin(np.maximum(t1, t2), 1)
-            hit = (tmax >= np.maximum(tmin, 0)) & (tmin > 0)
-            t = np.where(hit & (tmin < t), tmin, t)
+        # slab test of every ray against every box (float32, axis by axis);
+        # the nearest hit wins
+        lo = np.stack([boxes[:, 0] - boxes[:, 2], boxes[:, 1] - boxes[:, 3],
+                       np.full(len(boxes), -sensor_h)], -1).astype(np.float32)
+        hi = np.stack([boxes[:, 0] + boxes[:, 2], boxes[:, 1] + boxes[:, 3],
+                       -sensor_h + boxes[:, 4]], -1).astype(np.float32)
+        tmin = np.full((len(boxes), len(dirs)), -np.inf, np.float32)
+        tmax = np.full((len(boxes), len(dirs)), np.inf, np.float32)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            for a in range(3):
+                t1 = np.multiply.outer(lo[:, a], inv32[:, a])
+                t2 = np.multiply.outer(hi[:, a], inv32[:, a])
+                np.fmax(tmin, np.fmin(t1, t2), out=tmin)
+                np.fmin(tmax, np.fmax(t1, t2), out=tmax)
+        hit = (tmax >= np.maximum(tmin, 0)) & (tmin > 0)
+        tbox = np.where(hit, tmin, np.float32(np.inf)).min(0)
+        t = np.minimum(t, tbox.astype(np.float64))
         t = t + rng.normal(0, 0.02, len(t))
         xyz = (dirs * t[:, None]).astype(np.float32)
         mn = np.float32(xyz.min())
