@@ -223,93 +223,34 @@ __global__ void __launch_bounds__(1024)
 }
 
 // --------------------------------------------------------------- scatter --
-// Each chunk's keys go to its reserved ranges of the buckets in tiles of
-// kScTile keys: the tile's keys are ranked within their buckets (shared-
-// memory counters), staged in bucket order, and written out so that
-// consecutive threads write consecutive positions of a bucket's run (a few
-// keys per bucket per tile, instead of one scattered 4-byte store per key).
-constexpr int kScTile = 8192;
-constexpr int kScPer = kScTile / kLsThreads;
-
-size_t lsort_scatter_smem(int nb) {
-  return align_up(4 * (size_t)nb + 2 * ((size_t)kLcdfBlutSize + 1), 16) + 12 * (size_t)nb +
-         6 * (size_t)kScTile + 256;
-}
-
-__global__ void __launch_bounds__(kLsThreads, 1)
+__global__ void __launch_bounds__(kLsThreads, 2)
     lsort_scatter_kernel(const uint32_t* __restrict__ keys, int n, const char* __restrict__ blob,
                          LcdfLayout L, const uint32_t* __restrict__ chunk_off,
                          const uint32_t* __restrict__ starts, int nb, uint32_t* __restrict__ out,
                          const LsortStats* __restrict__ stats) {
   if (stats->skip) return;
   extern __shared__ __align__(16) unsigned char sm[];
-  uint32_t* s_bounds = reinterpret_cast<uint32_t*>(sm);
-  uint16_t* s_blut = reinterpret_cast<uint16_t*>(s_bounds + nb);
-  uint32_t* cursor = reinterpret_cast<uint32_t*>(
-      sm + align_up(4 * (size_t)nb + 2 * ((size_t)kLcdfBlutSize + 1), 16));
-  uint32_t* cnt = cursor + nb;    // per-tile counts, then the tile's bucket starts
-  uint32_t* gbase = cnt + nb;     // output position of staged slot 0 of each bucket
-  uint32_t* stage = gbase + nb;   // kScTile keys in bucket order
-  uint16_t* sbk = reinterpret_cast<uint16_t*>(stage + kScTile);  // their buckets
-  uint32_t* scratch = reinterpret_cast<uint32_t*>(sbk + kScTile);
-  const int tid = threadIdx.x;
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
   const int G = gridDim.x, c = blockIdx.x;
-  for (int b = tid; b < nb; b += kLsThreads) {
+  for (int b = threadIdx.x; b < nb; b += kLsThreads)
     cursor[b] = starts[b] + chunk_off[(size_t)c * nb + b];
-    cnt[b] = 0;
-  }
-  const BucketLookup q = load_lookup(blob, L, nb, s_bounds, s_blut);
+  const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
+                                     reinterpret_cast<uint16_t*>(cursor + 2 * nb));
   const int lo = (int)((long long)n * c / G), hi = (int)((long long)n * (c + 1) / G);
-  const int per = (nb + kLsThreads - 1) / kLsThreads;
-  for (int t0 = lo; t0 < hi; t0 += kScTile) {
-    const int tn = min(kScTile, hi - t0);
-    uint32_t key[kScPer], bk[kScPer], rk[kScPer];
+  for (int base = lo + threadIdx.x; base < hi; base += kLsUnroll * kLsThreads) {
+    uint32_t k[kLsUnroll];
 #pragma unroll
-    for (int u = 0; u < kScPer; ++u) {
-      const int i = u * kLsThreads + tid;
-      if (i < tn) key[u] = keys[t0 + i];
+    for (int u = 0; u < kLsUnroll; ++u) {
+      const int i = base + u * kLsThreads;
+      if (i < hi) k[u] = keys[i];
     }
 #pragma unroll
-    for (int u = 0; u < kScPer; ++u) {
-      if (u * kLsThreads + tid < tn) {
-        bk[u] = bucket_of(q, key[u]);
-        rk[u] = atomicAdd(&cnt[bk[u]], 1u);
+    for (int u = 0; u < kLsUnroll; ++u) {
+      if (base + u * kLsThreads < hi) {
+        const uint32_t pos = atomicAdd(&cursor[bucket_of(q, k[u])], 1u);
+        if (pos < (uint32_t)n) out[pos] = k[u];
       }
     }
-    __syncthreads();
-    uint32_t sum = 0;
-    for (int j = 0; j < per; ++j) {
-      const int b = tid * per + j;
-      if (b < nb) sum += cnt[b];
-    }
-    uint32_t ex = block_exclusive_sum<kLsThreads>(sum, scratch, scratch + 32);
-    for (int j = 0; j < per; ++j) {
-      const int b = tid * per + j;
-      if (b < nb) {
-        const uint32_t v = cnt[b];
-        gbase[b] = cursor[b] - ex;  // output position = gbase[b] + staged slot
-        cursor[b] += v;
-        cnt[b] = ex;
-        ex += v;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int u = 0; u < kScPer; ++u) {
-      if (u * kLsThreads + tid < tn) {
-        const uint32_t sp = cnt[bk[u]] + rk[u];
-        stage[sp] = key[u];
-        sbk[sp] = (uint16_t)bk[u];
-      }
-    }
-    __syncthreads();
-    for (int j = tid; j < tn; j += kLsThreads) {
-      const uint32_t pos = gbase[sbk[j]] + (uint32_t)j;
-      if (pos < (uint32_t)n) out[pos] = stage[j];
-    }
-    __syncthreads();
-    for (int b = tid; b < nb; b += kLsThreads) cnt[b] = 0;
-    __syncthreads();
   }
 }
 
@@ -704,11 +645,9 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(lsort_hist_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hsm);
-  const size_t ssm = lsort_scatter_smem(p.nb);
-  if (ssm > (size_t)kLsortMaxSmem) return cudaErrorInvalidValue;
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(lsort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)ssm);
+                             (int)hsm);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(lsort_bucket_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BucketSmem));
@@ -726,7 +665,7 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   lsort_offsets_kernel<<<(p.nb + 31) / 32, 256, 0, s>>>(hist, p.chunks, p.nb, totals);
   lsort_scan_kernel<<<1, 1024, 0, s>>>(totals, p.nb, n, threshold, blob, starts, stats);
   mark(rec, s);
-  lsort_scatter_kernel<<<p.chunks, kLsThreads, ssm, s>>>(keys, n, blob, p.L, hist, starts, p.nb,
+  lsort_scatter_kernel<<<p.chunks, kLsThreads, hsm, s>>>(keys, n, blob, p.L, hist, starts, p.nb,
                                                          bkeys, stats);
   mark(rec, s);
   lsort_bucket_kernel<<<p.nb, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, starts, ucount, stats);
@@ -778,8 +717,7 @@ LearnedBuildLayout learned_layout(int n, int cap, int nb, int max_segments) {
 bool lsort_args_ok(int n, int nb, int max_segments) {
   return n >= 0 && n <= OCT_MAX_N && nb >= 1 && nb <= 65536 && max_segments >= 1 &&
          max_segments <= octgb::kLcdfMaxSegments &&
-         octgb::lsort_hist_smem(nb, max_segments) <= (size_t)octgb::kLsortMaxSmem &&
-         octgb::lsort_scatter_smem(nb) <= (size_t)octgb::kLsortMaxSmem;
+         octgb::lsort_hist_smem(nb, max_segments) <= (size_t)octgb::kLsortMaxSmem;
 }
 
 int fail_cuda(cudaError_t e, const char* where) {

@@ -32,7 +32,6 @@ struct LsortPlan {
 
 LsortPlan lsort_plan(int n, int nb, int max_segments);
 size_t lsort_hist_smem(int nb, int max_segments);
-size_t lsort_scatter_smem(int nb);
 constexpr int kLsortMaxSmem = 227 * 1024;  // dynamic shared memory per CTA on sm_103
 
 // Sorted unique keys into `out`, U into *d_unique. With pts != nullptr the
