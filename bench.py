@@ -499,7 +499,7 @@ def batched_workload(dev, flush, reps):
     per-cloud plain loop."""
     import torch
 
-    from pipeline_gb300 import datasets
+    from pipeline_gb300 import autotune, datasets
     from pipeline_gb300.batch import BatchOctreeBuilder
     from pipeline_gb300.pipeline import OctreeBuilder
 
@@ -510,6 +510,16 @@ def batched_workload(dev, flush, reps):
     pts = torch.from_numpy(np.concatenate(clouds, 0)).to(dev)
     mins = torch.zeros(len(clouds), dtype=torch.float32, device=dev)
     ranges = torch.full((len(clouds),), RANGE, dtype=torch.float32, device=dev)
+    # sort shape for this batch chosen by the autotuner (batched plans use the
+    # tile-scan offsets, so only those candidates apply)
+    old_cfg = autotune.get_config()
+
+    def make_runner():
+        bb = BatchOctreeBuilder(sizes, device=dev)
+        return lambda: bb.build(pts, mins, ranges)
+
+    tuned = autotune.tune(make_runner, "batched", total, reps=3,
+                          candidates=[c for c in autotune.CANDIDATES if c[3] == 1], save=False)
     b = BatchOctreeBuilder(sizes, device=dev)
     b.capture(pts, mins, ranges)
     offs = np.concatenate([[0], np.cumsum(sizes)])
@@ -533,11 +543,14 @@ def batched_workload(dev, flush, reps):
         exact &= r["oct_nodes"].tobytes() == g["oct_nodes"].tobytes()
     t_batch = _time_events(b.replay, reps, stream, flush)
     t_loop = _time_events(loop, max(2, reps // 4), stream, flush)
+    autotune.set_config(old_cfg)
     return {"workload": "batched_512: 512 clouds, sizes log-uniform in [1K, 1M] (seed 11), even "
                         "uniform, odd 8-Gaussian mixtures; one CUDA-graph-captured batched build",
             "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
             "per_cloud_loop_mpts": round(total / t_loop / 1e3, 1),
-            "speedup": round(t_loop / t_batch, 3), "bit_exact_spot_check": bool(exact)}
+            "speedup": round(t_loop / t_batch, 3), "bit_exact_spot_check": bool(exact),
+            "autotuned_sort_shape": {"radix_bits": tuned["config"][0], "warps": tuned["config"][1],
+                                     "items": tuned["config"][2], "candidates_ms": tuned["all"]}}
 
 
 def frames_workload(dev, flush, reps):
