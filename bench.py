@@ -56,9 +56,9 @@ WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 
 # as fixed by the octree-build analysis: stage 1 reads 16 B and writes 4 B per
 # point (its digit histograms are fused, so the sort reads no extra 4 B/key);
 # each 10-bit sort pass reads and writes 4 B per key; unique reads 4 B per key
-# and writes 4 B per unique key; the radix tree reads 4 B per code and writes
-# 11 B per node; edge count + prefix sum read 1+4+1 B and write 4+4 B per
-# node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
+# and writes 4 B per unique key; the radix tree with its edge counts reads 4 B
+# per code and writes 15 B per node (11 B of tree + 4 B of edge count); the
+# prefix sum reads 4 B and writes 4 B per node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
 # leaf link (split over the emit and finalize launches).
 def algorithmic_bytes(n, u, b, m):
     leaves = b + 1
@@ -68,8 +68,8 @@ def algorithmic_bytes(n, u, b, m):
         "sort pass 1": 8 * n,
         "sort pass 2": 8 * n,
         "unique": 4 * n + 4 * u,
-        "radix tree": 4 * u + 11 * b,
-        "edge count+prefix sum": 14 * b,
+        "radix tree+edge count": 4 * u + 15 * b,
+        "prefix sum": 8 * b,
         "octree emit": 40 * b + 4 * leaves,
         "octree finalize": 60 * m,
     }
@@ -390,12 +390,13 @@ def run_ours(args, rank, world, local_rank):
 def build_launches() -> int:
     """Kernel launches of one plain build under the active sort shape:
     Morton, digit-base scan, per pass (tile histogram + tile scan +) pass,
-    unique, tree, edge count + scan, octree zero/emit/finalize, counts."""
+    unique, tree tiles + tree nodes, prefix sum, octree zero/emit/finalize,
+    counts."""
     from pipeline_gb300 import autotune
 
     rb, _, _, scan = autotune.get_config()
     passes = (30 + rb - 1) // rb
-    return 2 + passes * (3 if scan == 1 else 1) + 1 + 1 + 1 + 3 + 1
+    return 2 + passes * (3 if scan == 1 else 1) + 1 + 2 + 1 + 3 + 1
 
 
 def profile_only(args):
@@ -699,30 +700,34 @@ def sort_bar_workload(dev, flush, reps, pts):
 
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_uniform_4m.txt")
 TRAFFIC_POINTS = 4194304
-TRAFFIC_KERNELS = {"morton+histogram": "morton_kernel<10, 1>", "unique": "unique_kernel",
-                   "radix tree": "radix_tree_kernel", "edge count+prefix sum": "edge_scan_kernel",
-                   "octree zero": "oct_zero_kernel", "octree emit": "oct_emit_kernel",
-                   "octree finalize": "oct_finalize_kernel"}
+TRAFFIC_KERNELS = {"morton+histogram": ["morton_kernel<10, 1>"], "unique": ["unique_kernel"],
+                   "radix tree+edge count": ["tree_tiles_kernel", "tree_nodes_kernel"],
+                   "prefix sum": ["edge_scan_kernel"], "octree zero": ["oct_zero_kernel"],
+                   "octree emit": ["oct_emit_kernel"], "octree finalize": ["oct_finalize_kernel"]}
 
 
 def read_traffic(kernel_step: str, n: int):
-    """DRAM bytes (read + write) per launch of a kernel from the committed ncu
-    summary of the 4,194,304-point build, scaled to n points; None when the
-    summary does not cover it. At that size outputs may still sit in L2 when
-    a kernel ends, so this can fall below the algorithmic bytes."""
-    name = TRAFFIC_KERNELS.get(kernel_step)
-    if name is None or not os.path.exists(TRAFFIC_FILE):
+    """DRAM bytes (read + write) of one build step (the sum over its kernels)
+    from the committed ncu summary of the 4,194,304-point build, scaled to n
+    points; None when the summary does not cover every kernel of the step. At
+    that size outputs may still sit in L2 when a kernel ends, so this can fall
+    below the algorithmic bytes."""
+    names = TRAFFIC_KERNELS.get(kernel_step)
+    if not names or not os.path.exists(TRAFFIC_FILE):
         return None
+    found = {}
     with open(TRAFFIC_FILE) as f:
         for ln in f:
             parts = ln.split()
-            if len(parts) >= 4 and ln.strip().startswith(name):
-                try:
-                    mb = float(parts[-3]) + float(parts[-2])
-                except ValueError:
-                    continue
-                return int(mb * 1e6 * n / TRAFFIC_POINTS)
-    return None
+            for name in names:
+                if name not in found and len(parts) >= 4 and ln.strip().startswith(name):
+                    try:
+                        found[name] = float(parts[-3]) + float(parts[-2])
+                    except ValueError:
+                        pass
+    if len(found) != len(names):
+        return None
+    return int(sum(found.values()) * 1e6 * n / TRAFFIC_POINTS)
 
 
 def main():

@@ -171,6 +171,20 @@ OCT_API int oct_build_radix_tree(int n_nodes, const uint32_t* codes, uint8_t* pr
                          uint8_t* has_leaf_left, uint8_t* has_leaf_right, int32_t* left_child,
                          int32_t* parent, oct_stream_t stream);
 
+/* The same stage for strictly increasing codes below 2^31 (what stages 1-3 */
+/* produce), built from the deltas of adjacent codes instead of per-node     */
+/* searches; identical outputs for such codes (other inputs: unspecified     */
+/* values, no out-of-bounds access). With edge_count != NULL it also writes  */
+/* stage 5's edge counts (k_EdgeCount, include/kernels/05_edge_count.hpp:5-8)*/
+/* for the same tree. workspace: oct_radix_tree_sorted_workspace_bytes(),    */
+/* 256-byte aligned.                                                          */
+/* ----------------------------------------------------------------------- */
+OCT_API size_t oct_radix_tree_sorted_workspace_bytes(int n_nodes);
+OCT_API int oct_build_radix_tree_sorted(int n_nodes, const uint32_t* codes, uint8_t* prefix_n,
+                                uint8_t* has_leaf_left, uint8_t* has_leaf_right,
+                                int32_t* left_child, int32_t* parent, int32_t* edge_count,
+                                void* workspace, size_t workspace_bytes, oct_stream_t stream);
+
 /* ----------------------------------------------------------------------- */
 /* Stage 5: edge count. Replaces k_EdgeCount                                 */
 /* (include/kernels/05_edge_count.hpp:5-8): ec[0] = 0,                       */

@@ -83,6 +83,8 @@ SIGNATURES = {
     "oct_unique_workspace_bytes": (Z, [I]),
     "oct_unique": (I, [P, I, P, P, Z, P, P]),
     "oct_build_radix_tree": (I, [I, P, P, P, P, P, P, P]),
+    "oct_radix_tree_sorted_workspace_bytes": (Z, [I]),
+    "oct_build_radix_tree_sorted": (I, [I, P, P, P, P, P, P, P, P, Z, P]),
     "oct_edge_count": (I, [P, P, P, I, P]),
     "oct_prefix_sum_workspace_bytes": (Z, [I]),
     "oct_prefix_sum": (I, [P, I, P, P, Z, P, P]),

@@ -33,7 +33,7 @@ struct BuildLayout {
   SortPlan sort;
   ScanPlan uniq, scan;
   size_t sort_off, uniq_off, scan_off, misc_off, ctrl_bytes;
-  size_t keys_a_off, keys_b_off, tags_off, total;
+  size_t keys_a_off, keys_b_off, tree_off, tags_off, total;
 };
 
 BuildLayout build_layout(int n, int cap) {
@@ -51,7 +51,8 @@ BuildLayout build_layout(int n, int cap) {
   L.ctrl_bytes = L.sort_off + L.sort.zero_bytes;
   L.keys_a_off = align_up(L.sort_off + L.sort.bytes, 256);
   L.keys_b_off = align_up(L.keys_a_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
-  L.tags_off = align_up(L.keys_b_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
+  L.tree_off = align_up(L.keys_b_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
+  L.tags_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
   L.total = align_up(L.tags_off + oct_tags_bytes(cap), 256);
   return L;
 }
@@ -189,6 +190,28 @@ int oct_build_radix_tree(int n_nodes, const uint32_t* codes, uint8_t* prefix_n,
   OCT_TRY(launch_radix_tree(n_nodes, nullptr, codes, prefix_n, has_leaf_left, has_leaf_right,
                             left_child, parent, S(stream)),
           "oct_build_radix_tree");
+  return OCT_OK;
+}
+
+size_t oct_radix_tree_sorted_workspace_bytes(int n_nodes) {
+  if (n_nodes < 0 || n_nodes > OCT_MAX_N - 1) return 0;
+  return tree_scratch_bytes(n_nodes);
+}
+
+int oct_build_radix_tree_sorted(int n_nodes, const uint32_t* codes, uint8_t* prefix_n,
+                                uint8_t* has_leaf_left, uint8_t* has_leaf_right,
+                                int32_t* left_child, int32_t* parent, int32_t* edge_count,
+                                void* workspace, size_t workspace_bytes, oct_stream_t stream) {
+  if (n_nodes < 0 || n_nodes > OCT_MAX_N - 1) return OCT_ERR_INVALID_ARG;
+  if (n_nodes == 0) return OCT_OK;
+  if (!codes || !prefix_n || !has_leaf_left || !has_leaf_right || !left_child || !parent ||
+      !workspace || !aligned(workspace, 256))
+    return OCT_ERR_INVALID_ARG;
+  if (workspace_bytes < tree_scratch_bytes(n_nodes)) return OCT_ERR_WORKSPACE;
+  OCT_TRY(launch_radix_tree_sorted(n_nodes, nullptr, codes, prefix_n, has_leaf_left,
+                                   has_leaf_right, left_child, parent, edge_count, workspace,
+                                   S(stream)),
+          "oct_build_radix_tree_sorted");
   return OCT_OK;
 }
 
@@ -350,14 +373,17 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
   OCT_TRY(launch_unique(sorted, out->codes, n, m.unique, &L.uniq, w + L.uniq_off, m.status, s),
           "build: unique");
   mark(rec, s);
-  OCT_TRY(launch_radix_tree(n, m.unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
-                            out->tree.has_leaf_right, out->tree.left_child, out->tree.parent, s),
+  // The codes are the build's own sorted unique Morton codes: the tree comes
+  // from their adjacent deltas, with the edge counts.
+  OCT_TRY(launch_radix_tree_sorted(n, m.unique, out->codes, out->tree.prefix_n,
+                                   out->tree.has_leaf_left, out->tree.has_leaf_right,
+                                   out->tree.left_child, out->tree.parent, out->edge_count,
+                                   w + L.tree_off, s),
           "build: radix tree");
   mark(rec, s);
-  OCT_TRY(launch_edge_scan(kEdgeAndScan, n, m.unique, out->tree.prefix_n, out->tree.parent,
-                           out->edge_count, out->prefix_sum, m.max_slot, &L.scan, w + L.scan_off,
-                           m.status, s),
-          "build: edge count + prefix sum");
+  OCT_TRY(launch_edge_scan(kScanOnly, n, m.unique, nullptr, nullptr, out->edge_count,
+                           out->prefix_sum, m.max_slot, &L.scan, w + L.scan_off, m.status, s),
+          "build: prefix sum");
   mark(rec, s);
   if (out->nodes_capacity > 0) {
     OctArgs a{};
@@ -397,7 +423,7 @@ int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range
 
 static const char* const kBuildSteps[] = {
     "start",        "clear",         "morton+histogram", "histogram scan", "sort pass 0",
-    "sort pass 1",  "sort pass 2",   "unique",           "radix tree",     "edge count+prefix sum",
+    "sort pass 1",  "sort pass 2",   "unique",           "radix tree+edge count", "prefix sum",
     "octree zero",  "octree emit",   "octree finalize",  "publish counts"};
 
 int oct_build_step_count(void) { return (int)(sizeof(kBuildSteps) / sizeof(kBuildSteps[0])); }

@@ -109,6 +109,23 @@ cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* c
                               uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int* left_child,
                               int* parent, cudaStream_t s);
 
+// The same outputs for strictly increasing codes below 2^31 (the build's own
+// sorted unique Morton codes), from the adjacent deltas; with ec != nullptr
+// also the edge counts. scratch: tree_scratch_bytes(n_host), 256-aligned.
+struct TreeScratch {
+  uint8_t* D;          // [tiles * 4096] adjacent deltas
+  int* tile_last;      // [tiles * 32] last position of the tile with D < v, or -1
+  int* tile_first;     // [tiles * 32] first position of the tile with D < v, or INT_MAX
+  uint8_t* tile_min;   // [tiles rounded up to 512] smallest D of the tile
+  int tiles;
+};
+size_t tree_scratch_bytes(int n_host);
+TreeScratch tree_scratch_carve(void* base, int n_host);
+cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint32_t* codes,
+                                     uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
+                                     int* left_child, int* parent, int* ec, void* scratch,
+                                     cudaStream_t s);
+
 ScanPlan edge_scan_plan(int n);
 enum EdgeScanMode { kEdgeOnly = 1, kScanOnly = 2, kEdgeAndScan = 3 };
 // kEdgeOnly: ec = edge counts. kScanOnly: ps = inclusive scan of ec.

@@ -697,7 +697,7 @@ namespace {
 struct LearnedBuildLayout {
   octgb::LsortPlan lp;
   octgb::ScanPlan scan;
-  size_t misc_off, scan_off, lsort_off, keys_off, tags_off, total;
+  size_t misc_off, scan_off, lsort_off, keys_off, tree_off, tags_off, total;
 };
 
 LearnedBuildLayout learned_layout(int n, int cap, int nb, int max_segments) {
@@ -709,7 +709,8 @@ LearnedBuildLayout learned_layout(int n, int cap, int nb, int max_segments) {
   L.scan_off = 256;
   L.lsort_off = align_up(L.scan_off + L.scan.bytes, 256);
   L.keys_off = align_up(L.lsort_off + L.lp.bytes, 256);
-  L.tags_off = align_up(L.keys_off + 4 * (size_t)(n > 0 ? n : 1), 256);
+  L.tree_off = align_up(L.keys_off + 4 * (size_t)(n > 0 ? n : 1), 256);
+  L.tags_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
   L.total = align_up(L.tags_off + oct_tags_bytes(cap), 256);
   return L;
 }
@@ -814,12 +815,13 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
                      static_cast<const char*>(model), L.lp, w + L.lsort_off, overflow_threshold,
                      out->codes, d_unique, status, s, nullptr);
   if (e == cudaSuccess)
-    e = launch_radix_tree(n, d_unique, out->codes, out->tree.prefix_n, out->tree.has_leaf_left,
-                          out->tree.has_leaf_right, out->tree.left_child, out->tree.parent, s);
+    e = launch_radix_tree_sorted(n, d_unique, out->codes, out->tree.prefix_n,
+                                 out->tree.has_leaf_left, out->tree.has_leaf_right,
+                                 out->tree.left_child, out->tree.parent, out->edge_count,
+                                 w + L.tree_off, s);
   if (e == cudaSuccess)
-    e = launch_edge_scan(kEdgeAndScan, n, d_unique, out->tree.prefix_n, out->tree.parent,
-                         out->edge_count, out->prefix_sum, d_max_slot, &L.scan, w + L.scan_off,
-                         status, s);
+    e = launch_edge_scan(kScanOnly, n, d_unique, nullptr, nullptr, out->edge_count,
+                         out->prefix_sum, d_max_slot, &L.scan, w + L.scan_off, status, s);
   if (e == cudaSuccess && out->nodes_capacity > 0) {
     OctArgs a{};
     a.nodes = out->nodes;

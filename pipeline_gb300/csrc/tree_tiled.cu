@@ -1,0 +1,373 @@
+// Stage 4 (and stage 5's edge counts) for strictly increasing codes below
+// 2^31, from the deltas of adjacent codes.
+//
+// For such codes the radix tree of k_BuildRadixTree
+// (kernels/04_radix_tree.cpp:39-121) is the Cartesian tree of the adjacent
+// deltas D[q] = delta(codes[q], codes[q + 1]), q in [0, n): the node whose
+// split (gamma) is q covers the codes that share their first D[q] + 1 bits
+// with codes[q], i.e. [a + 1, b], where a is the nearest position left of q
+// with a smaller delta and b the nearest one right of q (-1 / n when there is
+// none). Its index is a + 1 when D[a] > D[b] (it is its parent's right child)
+// and b otherwise (the left child). Inside any node's range the smallest delta
+// occurs exactly once, so these are the ranges and splits the reference's
+// exact searches find. Only radix node 0 differs: the reference starts it at
+// d = 1, l = n - 1 (range [0, n - 1]), so its split is the smallest delta of
+// [0, n - 2] and its right end is n - 1. When that is not the overall
+// smallest delta (the delta at n - 1 is), the root is "short": node n - 1
+// covers the same range and the reference's node 0 writes no children's
+// parents.
+//
+// The parent of node i is the node split at a or b, whichever has the larger
+// delta, so the edge count prefix_n[i]/3 - prefix_n[parent[i]]/3
+// (kernels/05_edge_count.cpp:3-16) is computed here as well.
+//
+// Two kernels over tiles of 4,096 positions:
+//   tree_tiles_kernel  D as bytes; per tile, for every value v the first and
+//                      last position with D < v, and the tile's smallest D;
+//   tree_nodes_kernel  nearest smaller deltas inside each 32-position chunk
+//                      from five ballots over the bits of D, across the
+//                      tile's chunks from prefix / suffix tables in shared
+//                      memory, across tiles from the tile tables (rare: only
+//                      the tile's running minima); then every output of the
+//                      node split at each position.
+#include <climits>
+
+#include "tree.cuh"
+
+namespace octgb {
+
+constexpr int kTtTile = 4096;
+constexpr int kTtChunks = kTtTile / 32;
+constexpr int kTtAThreads = 256;
+constexpr int kTtBThreads = 512;
+constexpr int kTtBWarps = kTtBThreads / 32;
+constexpr int kTtChunksPerWarp = kTtChunks / kTtBWarps;  // 8
+constexpr int kTtMinBlock = 512;  // tiles per step of the cross-tile scan (32 lanes x 16 bytes)
+// D of a position past the last one (and of malformed pairs): never below a
+// query value, which is at most 30 for codes below 2^31.
+constexpr uint32_t kTtAbsent = 31;
+constexpr uint32_t kFull = 0xffffffffu;
+
+static int tt_tiles(int n) { return ((n > 1 ? n : 1) + kTtTile - 1) / kTtTile; }
+
+size_t tree_scratch_bytes(int n) {
+  const size_t t = (size_t)tt_tiles(n);
+  return align_up(t * kTtTile, 256) + 2 * align_up(t * 32 * sizeof(int), 256) +
+         align_up(align_up(t, kTtMinBlock), 256);
+}
+
+TreeScratch tree_scratch_carve(void* base, int n) {
+  const size_t t = (size_t)tt_tiles(n);
+  char* p = static_cast<char*>(base);
+  TreeScratch S;
+  S.tiles = (int)t;
+  S.D = reinterpret_cast<uint8_t*>(p);
+  p += align_up(t * kTtTile, 256);
+  S.tile_last = reinterpret_cast<int*>(p);
+  p += align_up(t * 32 * sizeof(int), 256);
+  S.tile_first = reinterpret_cast<int*>(p);
+  p += align_up(t * 32 * sizeof(int), 256);
+  S.tile_min = reinterpret_cast<uint8_t*>(p);
+  return S;
+}
+
+// Lanes whose 5-bit value (bits in b[0..4]) is below v.
+__device__ __forceinline__ uint32_t lanes_below(const uint32_t (&b)[5], uint32_t v) {
+  uint32_t eq = kFull, lt = 0;
+#pragma unroll
+  for (int k = 4; k >= 0; --k) {
+    if ((v >> k) & 1u) {
+      lt |= eq & ~b[k];
+      eq &= b[k];
+    } else {
+      eq &= ~b[k];
+    }
+  }
+  return lt;
+}
+
+__device__ __forceinline__ void value_ballots(uint32_t d, uint32_t (&b)[5]) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) b[k] = __ballot_sync(kFull, (d >> k) & 1u);
+}
+
+__device__ __forceinline__ uint32_t tt_delta(uint32_t a, uint32_t b) {
+  return min((uint32_t)delta_u8(a, b), kTtAbsent);
+}
+
+__global__ void __launch_bounds__(kTtAThreads)
+    tree_tiles_kernel(int n_host, const int* __restrict__ d_unique,
+                      const uint32_t* __restrict__ codes, TreeScratch S) {
+  constexpr int kWarps = kTtAThreads / 32;
+  __shared__ int s_last[kWarps][32], s_first[kWarps][32];
+  __shared__ uint32_t s_min[kWarps];
+  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
+  const int t = blockIdx.x;
+  const int t0 = t * kTtTile;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (t == 0) {  // whole blocks of the tile-minimum array; the padding never matches
+    const int pad = (int)align_up((size_t)S.tiles, kTtMinBlock);
+    for (int k = S.tiles + (int)threadIdx.x; k < pad; k += kTtAThreads)
+      S.tile_min[k] = (uint8_t)kTtAbsent;
+  }
+  int last = -1, first = INT_MAX;  // lane v: positions with D < v
+  uint32_t dmin = kTtAbsent;
+  if (t0 < n) {
+    for (int c = warp; c < kTtChunks; c += kWarps) {
+      const int p = t0 + 32 * c + lane;
+      uint32_t cp = 0;
+      if (p <= n) cp = codes[p];  // codes[0..n]
+      uint32_t cn = __shfl_down_sync(kFull, cp, 1);
+      if (lane == 31 && p + 1 <= n) cn = codes[p + 1];
+      const uint32_t d = p < n ? tt_delta(cp, cn) : kTtAbsent;
+      S.D[p] = (uint8_t)d;
+      dmin = min(dmin, d);
+      uint32_t b[5];
+      value_ballots(d, b);
+      const uint32_t lt = lanes_below(b, (uint32_t)lane);
+      if (lt) {
+        last = t0 + 32 * c + 31 - __clz(lt);
+        if (first == INT_MAX) first = t0 + 32 * c + __ffs(lt) - 1;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dmin = min(dmin, __shfl_xor_sync(kFull, dmin, o));
+  s_last[warp][lane] = last;
+  s_first[warp][lane] = first;
+  if (lane == 0) s_min[warp] = dmin;
+  __syncthreads();
+  if (warp == 0) {
+    int l = -1, f = INT_MAX;
+    uint32_t m = kTtAbsent;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      l = max(l, s_last[w][lane]);
+      f = min(f, s_first[w][lane]);
+      m = min(m, s_min[w]);
+    }
+    S.tile_last[t * 32 + lane] = l;
+    S.tile_first[t * 32 + lane] = f;
+    if (lane == 0) S.tile_min[t] = (uint8_t)m;
+  }
+}
+
+// Bit j set when byte j of w (16 bytes) is below x.
+__device__ __forceinline__ uint32_t bytes_below(const uint4& w, uint32_t x) {
+  const uint32_t v[4] = {w.x, w.y, w.z, w.w};
+  uint32_t m = 0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    if (((v[j >> 2] >> (8 * (j & 3))) & 0xffu) < x) m |= 1u << j;
+  return m;
+}
+
+// Largest tile <= hi whose smallest delta is below x, or -1 (whole warp).
+__device__ int tiles_scan_left(const uint8_t* __restrict__ tmin, int hi, uint32_t x, int lane) {
+  if (hi < 0) return -1;
+  for (int blk = hi / kTtMinBlock; blk >= 0; --blk) {
+    const uint4 w = reinterpret_cast<const uint4*>(tmin + (size_t)blk * kTtMinBlock)[lane];
+    uint32_t m = bytes_below(w, x);
+    const int base = blk * kTtMinBlock + lane * 16;
+    if (base > hi) m = 0;
+    else if (base + 15 > hi) m &= (2u << (hi - base)) - 1u;
+    const uint32_t any = __ballot_sync(kFull, m != 0);
+    if (any) {
+      const int L = 31 - __clz(any);
+      const uint32_t mL = __shfl_sync(kFull, m, L);
+      return blk * kTtMinBlock + L * 16 + 31 - __clz(mL);
+    }
+  }
+  return -1;
+}
+
+// Smallest tile >= lo whose smallest delta is below x, or -1 (whole warp).
+__device__ int tiles_scan_right(const uint8_t* __restrict__ tmin, int lo, int tiles, uint32_t x,
+                                int lane) {
+  const int blocks = (tiles + kTtMinBlock - 1) / kTtMinBlock;
+  for (int blk = lo / kTtMinBlock; blk < blocks; ++blk) {
+    const uint4 w = reinterpret_cast<const uint4*>(tmin + (size_t)blk * kTtMinBlock)[lane];
+    uint32_t m = bytes_below(w, x);
+    const int base = blk * kTtMinBlock + lane * 16;
+    if (base + 15 < lo) m = 0;
+    else if (base < lo) m &= ~((1u << (lo - base)) - 1u);
+    const uint32_t any = __ballot_sync(kFull, m != 0);
+    if (any) {
+      const int L = __ffs(any) - 1;
+      const uint32_t mL = __shfl_sync(kFull, m, L);
+      return blk * kTtMinBlock + L * 16 + __ffs(mL) - 1;
+    }
+  }
+  return -1;
+}
+
+struct TreeOut {
+  uint8_t* prefix_n;
+  uint8_t* hll;
+  uint8_t* hlr;
+  int* left_child;
+  int* parent;
+  int* ec;  // optional
+};
+
+// Radix node 0 as the reference builds it (range [0, n - 1]) with split q.
+__device__ __forceinline__ void emit_root(const TreeOut& o, int n, int q, uint32_t x,
+                                          bool short_root) {
+  const bool ll = q == 0, lr = q + 1 == n - 1;
+  o.prefix_n[0] = (uint8_t)x;
+  o.left_child[0] = q;
+  o.hll[0] = ll;
+  o.hlr[0] = lr;
+  o.parent[0] = 0;
+  if (short_root || lr) o.parent[n - 1] = 0;
+  if (!short_root) {
+    if (!ll) o.parent[q] = 0;
+    if (!lr && q + 1 < n) o.parent[q + 1] = 0;
+  }
+  if (o.ec) o.ec[0] = 0;
+}
+
+__global__ void __launch_bounds__(kTtBThreads)
+    tree_nodes_kernel(int n_host, const int* __restrict__ d_unique,
+                      const uint32_t* __restrict__ codes, TreeScratch S, TreeOut o) {
+  __shared__ __align__(16) uint8_t s_D[kTtTile];
+  __shared__ int16_t s_pl[kTtChunks][32];  // last tile position before the chunk with D < v
+  __shared__ int16_t s_sf[kTtChunks][32];  // first tile position after the chunk with D < v
+  __shared__ int16_t s_wl[kTtBWarps][32], s_wf[kTtBWarps][32];
+  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
+  const int t = blockIdx.x;
+  const int t0 = t * kTtTile;
+  if (t0 >= n) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (n < 2) {  // a single node: the reference's search steps
+    if (tid == 0) {
+      radix_node(0, n, GlobalCodes{codes}, o.prefix_n, o.hll, o.hlr, o.left_child, o.parent);
+      if (o.ec) o.ec[0] = 0;
+    }
+    return;
+  }
+  if (tid < kTtTile / 16)
+    reinterpret_cast<uint4*>(s_D)[tid] = reinterpret_cast<const uint4*>(S.D + t0)[tid];
+  __syncthreads();
+
+  const uint32_t below_me = (1u << lane) - 1u;
+  const uint32_t above_me = ~below_me << 1;  // lanes > lane (lane 31: none)
+  uint32_t x[kTtChunksPerWarp];
+  int psv[kTtChunksPerWarp], nsv[kTtChunksPerWarp], cf[kTtChunksPerWarp];
+  int run = -1;
+#pragma unroll
+  for (int k = 0; k < kTtChunksPerWarp; ++k) {
+    const int c = warp * kTtChunksPerWarp + k;
+    const uint32_t d = s_D[32 * c + lane];
+    uint32_t b[5];
+    value_ballots(d, b);
+    const uint32_t lt_own = lanes_below(b, d);
+    const uint32_t lt_lane = lanes_below(b, (uint32_t)lane);
+    const uint32_t l = lt_own & below_me, r = lt_own & above_me;
+    x[k] = d;
+    psv[k] = l ? 32 * c + 31 - __clz(l) : -1;
+    nsv[k] = r ? 32 * c + __ffs(r) - 1 : -1;
+    s_pl[c][lane] = (int16_t)run;
+    if (lt_lane) run = 32 * c + 31 - __clz(lt_lane);
+    cf[k] = lt_lane ? 32 * c + __ffs(lt_lane) - 1 : kTtTile;
+  }
+  int runf = kTtTile;
+#pragma unroll
+  for (int k = kTtChunksPerWarp - 1; k >= 0; --k) {
+    const int c = warp * kTtChunksPerWarp + k;
+    s_sf[c][lane] = (int16_t)runf;
+    runf = min(runf, cf[k]);
+  }
+  s_wl[warp][lane] = (int16_t)run;
+  s_wf[warp][lane] = (int16_t)runf;
+  __syncthreads();
+  {
+    int cl = -1, cr = kTtTile;
+    for (int w = 0; w < warp; ++w) cl = max(cl, (int)s_wl[w][lane]);
+    for (int w = warp + 1; w < kTtBWarps; ++w) cr = min(cr, (int)s_wf[w][lane]);
+#pragma unroll
+    for (int k = 0; k < kTtChunksPerWarp; ++k) {
+      const int c = warp * kTtChunksPerWarp + k;
+      s_pl[c][lane] = (int16_t)max((int)s_pl[c][lane], cl);
+      s_sf[c][lane] = (int16_t)min((int)s_sf[c][lane], cr);
+    }
+  }
+  __syncwarp();
+
+#pragma unroll
+  for (int k = 0; k < kTtChunksPerWarp; ++k) {
+    const int c = warp * kTtChunksPerWarp + k;
+    const int q = t0 + 32 * c + lane;
+    const bool live = q < n;
+    const uint32_t xv = x[k];
+    // -2: not in this tile
+    int a = -2, b = -2;
+    if (live) {
+      if (psv[k] >= 0) a = t0 + psv[k];
+      else if (s_pl[c][xv] >= 0) a = t0 + s_pl[c][xv];
+      if (nsv[k] >= 0) b = t0 + nsv[k];
+      else if (s_sf[c][xv] < kTtTile) b = t0 + s_sf[c][xv];
+      if (a == -2) {  // the previous tile first
+        if (t == 0) a = -1;
+        else if (S.tile_last[(t - 1) * 32 + xv] >= 0) a = S.tile_last[(t - 1) * 32 + xv];
+      }
+      if (b == -2) {
+        if (t + 1 >= S.tiles) b = n;
+        else if (S.tile_first[(t + 1) * 32 + xv] != INT_MAX) b = S.tile_first[(t + 1) * 32 + xv];
+      }
+    }
+    // Farther tiles: one warp-wide scan of the tile minima per query.
+    uint32_t need = __ballot_sync(kFull, live && a == -2);
+    while (need) {
+      const int src = __ffs(need) - 1;
+      need &= need - 1;
+      const uint32_t qx = __shfl_sync(kFull, xv, src);
+      const int tt = tiles_scan_left(S.tile_min, t - 2, qx, lane);
+      const int ans = tt >= 0 ? S.tile_last[tt * 32 + qx] : -1;
+      if (lane == src) a = ans;
+    }
+    need = __ballot_sync(kFull, live && b == -2);
+    while (need) {
+      const int src = __ffs(need) - 1;
+      need &= need - 1;
+      const uint32_t qx = __shfl_sync(kFull, xv, src);
+      const int tt = tiles_scan_right(S.tile_min, t + 2, S.tiles, qx, lane);
+      const int ans = tt >= 0 ? S.tile_first[tt * 32 + qx] : n;
+      if (lane == src) b = ans;
+    }
+    if (!live) continue;
+    const int da = a < 0 ? -1 : (a >= t0 ? (int)s_D[a - t0] : (int)S.D[a]);
+    const int db = b >= n ? -1 : (b < t0 + kTtTile ? (int)s_D[b - t0] : (int)S.D[b]);
+    if (a < 0 && b >= n) {  // the smallest delta overall
+      if (q <= n - 2) emit_root(o, n, q, xv, false);
+      continue;             // at n - 1: the root is short; node 0 comes from [0, n - 2]'s split
+    }
+    const int i = a < 0 ? b : (b >= n ? a + 1 : (da > db ? a + 1 : b));
+    const bool ll = a + 1 == q, lr = b == q + 1;
+    const bool short_root = a < 0 && b == n - 1;
+    o.prefix_n[i] = (uint8_t)xv;
+    o.left_child[i] = q;
+    o.hll[i] = ll;
+    o.hlr[i] = lr;
+    if (!ll) o.parent[q] = i;
+    if (!lr) o.parent[q + 1] = i;
+    if (o.ec) o.ec[i] = short_root ? 0 : (int)(xv / 3) - max(da, db) / 3;
+    if (short_root) emit_root(o, n, q, xv, true);
+  }
+}
+
+cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint32_t* codes,
+                                     uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
+                                     int* left_child, int* parent, int* ec, void* scratch,
+                                     cudaStream_t s) {
+  if (n_host <= 0) return cudaSuccess;
+  const TreeScratch S = tree_scratch_carve(scratch, n_host);
+  tree_tiles_kernel<<<S.tiles, kTtAThreads, 0, s>>>(n_host, d_unique, codes, S);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
+  tree_nodes_kernel<<<S.tiles, kTtBThreads, 0, s>>>(n_host, d_unique, codes, S, o);
+  return cudaGetLastError();
+}
+
+}  // namespace octgb

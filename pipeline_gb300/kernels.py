@@ -147,6 +147,26 @@ def k_BuildRadixTree(n: int, codes: torch.Tensor, prefix_n: torch.Tensor,
         _stream()), "k_BuildRadixTree")
 
 
+def build_radix_tree_sorted(n: int, codes: torch.Tensor, prefix_n: torch.Tensor,
+                            has_leaf_left: torch.Tensor, has_leaf_right: torch.Tensor,
+                            left_child: torch.Tensor, parent: torch.Tensor,
+                            edge_count: torch.Tensor | None = None):
+    """Stage 4 (and, with ``edge_count``, stage 5) for strictly increasing
+    codes below 2^31, from the deltas of adjacent codes: the outputs of
+    k_BuildRadixTree (include/kernels/04_radix_tree.hpp:5-11) and k_EdgeCount
+    (include/kernels/05_edge_count.hpp:5-8) for such codes."""
+    lib = _lib.load()
+    ws_bytes = lib.oct_radix_tree_sorted_workspace_bytes(n)
+    ws = _workspace(ws_bytes, codes.device)
+    ec = _ptr(edge_count, "edge_count", torch.int32, n)
+    _lib.check(lib.oct_build_radix_tree_sorted(
+        n, _ptr(codes, "codes", torch.int32, n + 1), _ptr(prefix_n, "prefix_n", torch.uint8, n),
+        _ptr(has_leaf_left, "has_leaf_left", torch.uint8, n),
+        _ptr(has_leaf_right, "has_leaf_right", torch.uint8, n),
+        _ptr(left_child, "left_child", torch.int32, n), _ptr(parent, "parent", torch.int32, n),
+        ec, C.c_void_p(ws.data_ptr()), ws_bytes, _stream()), "build_radix_tree_sorted")
+
+
 # ------------------------------------------------------------------ stage 5 --
 def k_EdgeCount(prefix_n: torch.Tensor, parents: torch.Tensor, edge_count: torch.Tensor,
                 n_brt_nodes: int):
