@@ -347,12 +347,15 @@ def run_ours(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         pipe_ms = float(t.item())
     assert all(r[2] == m and r[3] == 0 for r in res)
+    del pb
+    link = host_link_bound(dev, pinned, outs[0], n * 16, m * 60)
     e2e = {"value": n * world / (pipe_ms / 1e3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": n * 16,
            "d2h_bytes_per_step": m * 60 + 16, "ms_per_step": round(pipe_ms, 4),
            "mode": "pipelined: upload, build and download of consecutive steps overlap "
                    "(3 streams, 3 slots)",
-           "serial_value": round(serial_mpts, 2), "serial_ms_per_step": round(e2e_ms, 4)}
-    del pb, outs
+           "serial_value": round(serial_mpts, 2), "serial_ms_per_step": round(e2e_ms, 4),
+           "link": dict(link, frac=round(link["both_ms"] / pipe_ms, 3))}
+    del outs
 
     workloads = {}
     if not args.no_extra:
@@ -385,6 +388,52 @@ def run_ours(args, rank, world, local_rank):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def host_link_bound(dev, pinned_in, pinned_out, in_bytes: int, out_bytes: int) -> dict:
+    """The host link alone, on one step's bytes: the points upload, the
+    OctNode download, and both at once on two streams (the pipelined
+    end-to-end step's floor). Best of 5 after 2 warm-up copies."""
+    import torch
+
+    src = pinned_in.view(-1).view(torch.uint8)[:in_bytes]
+    dst_h = pinned_out.view(-1).view(torch.uint8)[:out_bytes]
+    d_in = torch.empty(in_bytes, dtype=torch.uint8, device=dev)
+    d_out = torch.zeros(out_bytes, dtype=torch.uint8, device=dev)
+    s_a, s_b = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def timed(fn):
+        best = float("inf")
+        for r in range(7):
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            if r >= 2:
+                best = min(best, e0.elapsed_time(e1))
+        return best
+
+    def both():
+        cur = torch.cuda.current_stream(dev)
+        s_a.wait_stream(cur)
+        s_b.wait_stream(cur)
+        with torch.cuda.stream(s_a):
+            d_in.copy_(src, non_blocking=True)
+        with torch.cuda.stream(s_b):
+            dst_h.copy_(d_out, non_blocking=True)
+        cur.wait_stream(s_a)
+        cur.wait_stream(s_b)
+
+    h2d = timed(lambda: d_in.copy_(src, non_blocking=True))
+    d2h = timed(lambda: dst_h.copy_(d_out, non_blocking=True))
+    both_ms = timed(both)
+    del d_in, d_out
+    return {"h2d_ms": round(h2d, 4), "h2d_gbs": round(in_bytes / h2d / 1e6, 1),
+            "d2h_ms": round(d2h, 4), "d2h_gbs": round(out_bytes / d2h / 1e6, 1),
+            "both_ms": round(both_ms, 4), "both_gbs": round((in_bytes + out_bytes) / both_ms / 1e6, 1)}
 
 
 def build_launches() -> int:

@@ -154,9 +154,10 @@ __device__ __forceinline__ uint32_t morton_code(float x, float y, float z, float
 // morton32_to_xyz: per axis (raw / 1024) * range + min, w = 1.
 __device__ __forceinline__ float4 decode_corner(uint32_t code, float min_coord, float range) {
   float4 c;
-  c.x = __fadd_rn(__fmul_rn(__fdiv_rn((float)compact3(code), 1024.0f), range), min_coord);
-  c.y = __fadd_rn(__fmul_rn(__fdiv_rn((float)compact3(code >> 1), 1024.0f), range), min_coord);
-  c.z = __fadd_rn(__fmul_rn(__fdiv_rn((float)compact3(code >> 2), 1024.0f), range), min_coord);
+  // v / 1024 for an integer v < 1024 is exact, so it is the product v * 2^-10.
+  c.x = __fadd_rn(__fmul_rn(__fmul_rn((float)compact3(code), 0x1p-10f), range), min_coord);
+  c.y = __fadd_rn(__fmul_rn(__fmul_rn((float)compact3(code >> 1), 0x1p-10f), range), min_coord);
+  c.z = __fadd_rn(__fmul_rn(__fmul_rn((float)compact3(code >> 2), 0x1p-10f), range), min_coord);
   c.w = 1.0f;
   return c;
 }

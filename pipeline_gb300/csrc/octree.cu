@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctT
 }
 
 __global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
-  __shared__ int s_nodes[kFinThreads * kNodeWords];
+  __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
   const Sizes z = read_sizes(a);
   if (!z.fits || z.n_brt < 1) return;
   const int root_level = a.prefix_n[0] / 3;
@@ -84,7 +84,18 @@ __global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, Oct
     if (p < z.n_oct) finalize_slot(fresh, p, a, t, root_level, s_nodes + threadIdx.x * kNodeWords);
     __syncthreads();
     int* dst = out_words + (size_t)blk * kNodeWords;
-    for (int k = threadIdx.x; k < count * kNodeWords; k += kFinThreads) dst[k] = s_nodes[k];
+    // 256 nodes are 960 16-byte words; blk is a multiple of 256, so dst is
+    // 16-byte aligned whenever the node array is.
+    const int words = count * kNodeWords;
+    int k0 = 0;
+    if ((reinterpret_cast<uintptr_t>(a.nodes) & 15) == 0) {
+      const int quads = words >> 2;
+      const uint4* src4 = reinterpret_cast<const uint4*>(s_nodes);
+      uint4* dst4 = reinterpret_cast<uint4*>(dst);
+      for (int k = threadIdx.x; k < quads; k += kFinThreads) dst4[k] = src4[k];
+      k0 = quads << 2;
+    }
+    for (int k = k0 + threadIdx.x; k < words; k += kFinThreads) dst[k] = s_nodes[k];
     __syncthreads();
   }
 }

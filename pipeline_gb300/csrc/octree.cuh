@@ -149,6 +149,14 @@ __device__ __forceinline__ void emit_node(int mode, int i, const OctArgs& a, con
   }
 }
 
+// range / 2^k as the reference computes it (float division by (float)(1 << k)).
+// For k in [0, 30] the divisor is the exact power of two, and the correctly
+// rounded quotient equals the correctly rounded product range * 2^-k.
+__device__ __forceinline__ float cell_size(float range, int k) {
+  if (k >= 0 && k <= 30) return __fmul_rn(range, __int_as_float((127 - k) << 23));
+  return __fdiv_rn(range, (float)(1 << k));
+}
+
 // One thread per slot computes the node; the block stages its 256 nodes
 // (15 KB) in shared memory and writes them as consecutive 32-bit words, so
 // every warp store is one contiguous 128-byte line.
@@ -203,7 +211,7 @@ __device__ __forceinline__ void finalize_slot(bool fresh, int p, const OctArgs& 
     const int level = own_pn / 3 - j;
     const int sh = 30 - 3 * level;
     corner = decode_corner((own_code >> sh) << sh, a.min_coord, a.range);
-    cell = __fdiv_rn(a.range, (float)(1 << (level - root_level)));
+    cell = cell_size(a.range, level - root_level);
   } else if (fresh && p == 0) {
     const int sh = 30 - 3 * root_level;
     corner = decode_corner((a.codes[0] >> sh) << sh, a.min_coord, a.range);

@@ -71,19 +71,21 @@ TreeScratch tree_scratch_carve(void* base, int n) {
   return S;
 }
 
-// Lanes whose 5-bit value (bits in b[0..4]) is below v.
-__device__ __forceinline__ uint32_t lanes_below(const uint32_t (&b)[5], uint32_t v) {
+// Lanes whose 5-bit value is below v, from the ballots b[k] of the values'
+// bits and v's bits as masks (m[k] all ones where v has bit k).
+__device__ __forceinline__ uint32_t lanes_below(const uint32_t (&b)[5], const uint32_t (&m)[5]) {
   uint32_t eq = kFull, lt = 0;
 #pragma unroll
   for (int k = 4; k >= 0; --k) {
-    if ((v >> k) & 1u) {
-      lt |= eq & ~b[k];
-      eq &= b[k];
-    } else {
-      eq &= ~b[k];
-    }
+    lt |= eq & ~b[k] & m[k];
+    eq &= ~(b[k] ^ m[k]);
   }
   return lt;
+}
+
+__device__ __forceinline__ void bit_masks(uint32_t v, uint32_t (&m)[5]) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) m[k] = 0u - ((v >> k) & 1u);
 }
 
 __device__ __forceinline__ void value_ballots(uint32_t d, uint32_t (&b)[5]) {
@@ -113,21 +115,33 @@ __global__ void __launch_bounds__(kTtAThreads)
   int last = -1, first = INT_MAX;  // lane v: positions with D < v
   uint32_t dmin = kTtAbsent;
   if (t0 < n) {
-    for (int c = warp; c < kTtChunks; c += kWarps) {
-      const int p = t0 + 32 * c + lane;
-      uint32_t cp = 0;
-      if (p <= n) cp = codes[p];  // codes[0..n]
-      uint32_t cn = __shfl_down_sync(kFull, cp, 1);
-      if (lane == 31 && p + 1 <= n) cn = codes[p + 1];
-      const uint32_t d = p < n ? tt_delta(cp, cn) : kTtAbsent;
-      S.D[p] = (uint8_t)d;
-      dmin = min(dmin, d);
-      uint32_t b[5];
-      value_ballots(d, b);
-      const uint32_t lt = lanes_below(b, (uint32_t)lane);
-      if (lt) {
-        last = t0 + 32 * c + 31 - __clz(lt);
-        if (first == INT_MAX) first = t0 + 32 * c + __ffs(lt) - 1;
+    uint32_t lm[5];
+    bit_masks((uint32_t)lane, lm);
+    constexpr int kStep = 4;  // chunks whose codes are loaded together
+    for (int c0 = warp; c0 < kTtChunks; c0 += kWarps * kStep) {
+      uint32_t cp[kStep], cx[kStep];
+#pragma unroll
+      for (int j = 0; j < kStep; ++j) {
+        const int p = t0 + 32 * (c0 + j * kWarps) + lane;
+        cp[j] = p <= n ? codes[p] : 0u;  // codes[0..n]
+        cx[j] = (lane == 31 && p + 1 <= n) ? codes[p + 1] : 0u;
+      }
+#pragma unroll
+      for (int j = 0; j < kStep; ++j) {
+        const int c = c0 + j * kWarps;
+        const int p = t0 + 32 * c + lane;
+        uint32_t cn = __shfl_down_sync(kFull, cp[j], 1);
+        if (lane == 31) cn = cx[j];
+        const uint32_t d = p < n ? tt_delta(cp[j], cn) : kTtAbsent;
+        S.D[p] = (uint8_t)d;
+        dmin = min(dmin, d);
+        uint32_t b[5];
+        value_ballots(d, b);
+        const uint32_t lt = lanes_below(b, lm);
+        if (lt) {
+          last = t0 + 32 * c + 31 - __clz(lt);
+          if (first == INT_MAX) first = t0 + 32 * c + __ffs(lt) - 1;
+        }
       }
     }
   }
@@ -234,6 +248,7 @@ __global__ void __launch_bounds__(kTtBThreads)
   __shared__ int16_t s_pl[kTtChunks][32];  // last tile position before the chunk with D < v
   __shared__ int16_t s_sf[kTtChunks][32];  // first tile position after the chunk with D < v
   __shared__ int16_t s_wl[kTtBWarps][32], s_wf[kTtBWarps][32];
+  __shared__ uint8_t s_pv[kTtTile], s_nv[kTtTile];  // nearest smaller lane in the chunk, or 0xFF
   const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
   const int t = blockIdx.x;
   const int t0 = t * kTtTile;
@@ -252,21 +267,22 @@ __global__ void __launch_bounds__(kTtBThreads)
 
   const uint32_t below_me = (1u << lane) - 1u;
   const uint32_t above_me = ~below_me << 1;  // lanes > lane (lane 31: none)
-  uint32_t x[kTtChunksPerWarp];
-  int psv[kTtChunksPerWarp], nsv[kTtChunksPerWarp], cf[kTtChunksPerWarp];
+  uint32_t lm[5];
+  bit_masks((uint32_t)lane, lm);
+  int cf[kTtChunksPerWarp];
   int run = -1;
 #pragma unroll
   for (int k = 0; k < kTtChunksPerWarp; ++k) {
     const int c = warp * kTtChunksPerWarp + k;
     const uint32_t d = s_D[32 * c + lane];
-    uint32_t b[5];
+    uint32_t b[5], dm[5];
     value_ballots(d, b);
-    const uint32_t lt_own = lanes_below(b, d);
-    const uint32_t lt_lane = lanes_below(b, (uint32_t)lane);
+    bit_masks(d, dm);
+    const uint32_t lt_own = lanes_below(b, dm);
+    const uint32_t lt_lane = lanes_below(b, lm);
     const uint32_t l = lt_own & below_me, r = lt_own & above_me;
-    x[k] = d;
-    psv[k] = l ? 32 * c + 31 - __clz(l) : -1;
-    nsv[k] = r ? 32 * c + __ffs(r) - 1 : -1;
+    s_pv[32 * c + lane] = l ? (uint8_t)(31 - __clz(l)) : (uint8_t)0xFF;
+    s_nv[32 * c + lane] = r ? (uint8_t)(__ffs(r) - 1) : (uint8_t)0xFF;
     s_pl[c][lane] = (int16_t)run;
     if (lt_lane) run = 32 * c + 31 - __clz(lt_lane);
     cf[k] = lt_lane ? 32 * c + __ffs(lt_lane) - 1 : kTtTile;
@@ -294,18 +310,19 @@ __global__ void __launch_bounds__(kTtBThreads)
   }
   __syncwarp();
 
-#pragma unroll
+#pragma unroll 1
   for (int k = 0; k < kTtChunksPerWarp; ++k) {
     const int c = warp * kTtChunksPerWarp + k;
     const int q = t0 + 32 * c + lane;
     const bool live = q < n;
-    const uint32_t xv = x[k];
+    const uint32_t xv = s_D[32 * c + lane];
+    const uint32_t pv = s_pv[32 * c + lane], nv = s_nv[32 * c + lane];
     // -2: not in this tile
     int a = -2, b = -2;
     if (live) {
-      if (psv[k] >= 0) a = t0 + psv[k];
+      if (pv != 0xFF) a = t0 + 32 * c + (int)pv;
       else if (s_pl[c][xv] >= 0) a = t0 + s_pl[c][xv];
-      if (nsv[k] >= 0) b = t0 + nsv[k];
+      if (nv != 0xFF) b = t0 + 32 * c + (int)nv;
       else if (s_sf[c][xv] < kTtTile) b = t0 + s_sf[c][xv];
       if (a == -2) {  // the previous tile first
         if (t == 0) a = -1;
