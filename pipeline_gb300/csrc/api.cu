@@ -31,8 +31,8 @@ cudaStream_t S(oct_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 // Control block shared by the whole build: zeroed by one memset per build.
 struct BuildLayout {
   SortPlan sort;
-  ScanPlan uniq, scan;
-  size_t sort_off, uniq_off, scan_off, misc_off, ctrl_bytes;
+  ScanPlan uniq;
+  size_t sort_off, uniq_off, misc_off, ctrl_bytes;
   size_t keys_a_off, keys_b_off, tree_off, tags_off, total;
 };
 
@@ -40,13 +40,11 @@ BuildLayout build_layout(int n, int cap) {
   BuildLayout L{};
   L.sort = sort_plan(n, 30);
   L.uniq = unique_plan(n);
-  L.scan = edge_scan_plan(n);
   // Everything that must start at zero is contiguous from offset 0 up to the
   // end of the sort's zeroed part; the sort's digit bases and per-tile
   // histograms (always fully written before use) follow.
   L.uniq_off = 0;
-  L.scan_off = align_up(L.uniq_off + L.uniq.bytes, 256);
-  L.misc_off = align_up(L.scan_off + L.scan.bytes, 256);
+  L.misc_off = align_up(L.uniq_off + L.uniq.bytes, 256);
   L.sort_off = align_up(L.misc_off + 256, 256);
   L.ctrl_bytes = L.sort_off + L.sort.zero_bytes;
   L.keys_a_off = align_up(L.sort_off + L.sort.bytes, 256);
@@ -381,8 +379,9 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
                                    w + L.tree_off, s),
           "build: radix tree");
   mark(rec, s);
-  OCT_TRY(launch_edge_scan(kScanOnly, n, m.unique, nullptr, nullptr, out->edge_count,
-                           out->prefix_sum, m.max_slot, &L.scan, w + L.scan_off, m.status, s),
+  const OctTags tags = oct_tags_carve(w + L.tags_off, out->nodes_capacity);
+  OCT_TRY(launch_prefix_sum_clear_tags(n, m.unique, out->edge_count, out->prefix_sum, m.max_slot,
+                                       w + L.tree_off, m.status, tags, s),
           "build: prefix sum");
   mark(rec, s);
   if (out->nodes_capacity > 0) {
@@ -402,11 +401,10 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
     a.n_brt_host = n;
     a.d_unique = m.unique;
     a.d_max_slot = m.max_slot;
-    const OctTags t = oct_tags_carve(w + L.tags_off, out->nodes_capacity);
-    OCT_TRY(launch_octree(kOctMake | kOctLink | kOctFresh, a, t, m.status, s, rec),
+    OCT_TRY(launch_octree(kOctMake | kOctLink | kOctFresh, a, tags, m.status, s, rec, true),
             "build: octree");
   } else {
-    for (int k = 0; k < 3; ++k) mark(rec, s);
+    for (int k = 0; k < 2; ++k) mark(rec, s);
   }
   OCT_TRY(launch_publish_counts(m.unique, m.max_slot, m.status, out->d_counts, s),
           "build: counts");
@@ -424,7 +422,7 @@ int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range
 static const char* const kBuildSteps[] = {
     "start",        "clear",         "morton+histogram", "histogram scan", "sort pass 0",
     "sort pass 1",  "sort pass 2",   "unique",           "radix tree+edge count", "prefix sum",
-    "octree zero",  "octree emit",   "octree finalize",  "publish counts"};
+    "octree emit",  "octree finalize",  "publish counts"};
 
 int oct_build_step_count(void) { return (int)(sizeof(kBuildSteps) / sizeof(kBuildSteps[0])); }
 

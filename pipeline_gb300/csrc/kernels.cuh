@@ -117,6 +117,8 @@ struct TreeScratch {
   int* tile_last;      // [tiles * 32] last position of the tile with D < v, or -1
   int* tile_first;     // [tiles * 32] first position of the tile with D < v, or INT_MAX
   uint8_t* tile_min;   // [tiles rounded up to 512] smallest D of the tile
+  int* tile_sum;       // [tiles] sum of the edge counts of the tile's 4,096 nodes
+  uint32_t* tile_prefix;  // [tiles] exclusive prefix of tile_sum
   int tiles;
 };
 size_t tree_scratch_bytes(int n_host);
@@ -164,8 +166,18 @@ struct OctArgs {
   int n_oct_host;          // used when d_max_slot == nullptr
   const int* d_max_slot;   // largest slot on the device (n_oct = max_slot + 1)
 };
+// tags_clear: the tags of [0, M) are already zero (launch_prefix_sum_clear_tags).
 cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t* status,
-                          cudaStream_t s, Recorder* rec = nullptr);
+                          cudaStream_t s, Recorder* rec = nullptr, bool tags_clear = false);
+
+// Inclusive prefix sum of the edge counts written by launch_radix_tree_sorted
+// (which also summed them per 4,096-node tile into the scratch) that also
+// clears the octree tags of every slot stages 7-8 can touch, up to the tags'
+// capacity: one small kernel scans the tile sums, then every tile scans its
+// own nodes from its prefix (no inter-tile waits).
+cudaError_t launch_prefix_sum_clear_tags(int n_host, const int* d_unique, int* ec, int* ps,
+                                         int* d_max_slot, void* tree_scratch, uint32_t* status,
+                                         const OctTags& tags, cudaStream_t s);
 
 // Copies U, B, M, status into out[4] (device).
 cudaError_t launch_publish_counts(const int* d_unique, const int* d_max_slot,

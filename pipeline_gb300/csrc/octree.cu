@@ -63,9 +63,13 @@ __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
 }
 
 __global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctTags t,
-                                                       uint32_t* __restrict__ status) {
+                                                       uint32_t* __restrict__ status,
+                                                       bool report_capacity) {
   const Sizes z = read_sizes(a);
-  if (!z.fits) return;
+  if (!z.fits) {
+    if (report_capacity && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, kStatusCapacity);
+    return;
+  }
   const int stride = gridDim.x * blockDim.x;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < z.n_brt; i += stride)
     emit_node(mode, i, a, t, z, status);
@@ -101,17 +105,19 @@ __global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, Oct
 }
 
 cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t* status,
-                          cudaStream_t s, Recorder* rec) {
-  const int sms = device_sm_count();
-  const int zgrid = sms * 8;
-  oct_zero_kernel<<<zgrid, 256, 0, s>>>(a, t, status);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  mark(rec, s);
+                          cudaStream_t s, Recorder* rec, bool tags_clear) {
+  cudaError_t e;
+  if (!tags_clear) {
+    const int zgrid = device_sm_count() * 8;
+    oct_zero_kernel<<<zgrid, 256, 0, s>>>(a, t, status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    mark(rec, s);
+  }
   int nb = a.d_unique ? a.n_brt_host : a.n_brt_host;
   int egrid = (nb + 255) / 256;
   if (egrid < 1) egrid = 1;
-  oct_emit_kernel<<<egrid, 256, 0, s>>>(mode, a, t, status);
+  oct_emit_kernel<<<egrid, 256, 0, s>>>(mode, a, t, status, tags_clear);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(rec, s);

@@ -169,14 +169,17 @@ __global__ void __launch_bounds__(kEsThreads)
                      const uint8_t* __restrict__ prefix_n, const int* __restrict__ parent,
                      int* ec_out, int* __restrict__ ps_out, int* __restrict__ d_max_slot,
                      unsigned long long* __restrict__ lb, uint32_t* __restrict__ counter,
-                     uint32_t* __restrict__ status) {
+                     uint32_t* __restrict__ status, OctTags zt,
+                     const uint32_t* __restrict__ tile_prefix) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_misc[4];
   __shared__ int s_max[kEsThreads / 32];
+  __shared__ int s_hi;
   const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
   const int tid = threadIdx.x;
   // Edge count alone has no cross-tile dependency: the block index is the tile.
-  if (tid == 0) s_misc[0] = mode == kEdgeOnly ? blockIdx.x : atomicAdd(counter, 1u);
+  if (tid == 0)
+    s_misc[0] = (mode == kEdgeOnly || tile_prefix) ? blockIdx.x : atomicAdd(counter, 1u);
   __syncthreads();
   const int tile = (int)s_misc[0];
   const int start = tile * kEsTile;
@@ -258,7 +261,9 @@ __global__ void __launch_bounds__(kEsThreads)
 #pragma unroll
   for (int k = 0; k < kEsItems; ++k) sum += (uint32_t)v[k];
   const uint32_t off = block_exclusive_sum<kEsThreads>(sum, s_warp, &s_misc[2]);
-  if (tid < 32) {
+  if (tile_prefix) {  // tile prefixes known in advance
+    if (tid == 0) s_misc[3] = tile_prefix[tile];
+  } else if (tid < 32) {
     const uint32_t e = warp_lookback_u32(lb, tile, s_misc[2], status);
     if (tid == 0) s_misc[3] = e;
   }
@@ -296,7 +301,7 @@ __global__ void __launch_bounds__(kEsThreads)
       }
     }
   }
-  if (d_max_slot) {
+  if (d_max_slot || zt.child) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((tid & 31) == 0) s_max[tid >> 5] = mx;
@@ -304,7 +309,24 @@ __global__ void __launch_bounds__(kEsThreads)
     if (tid == 0) {
       int m = 0;
       for (int w = 0; w < kEsThreads / 32; ++w) m = max(m, s_max[w]);
-      atomicMax(d_max_slot, m);
+      if (d_max_slot) atomicMax(d_max_slot, m);
+      // The tile's octree slots: from its exclusive prefix (the slot after the
+      // previous tile's last prefix) to its largest slot or its last prefix.
+      s_hi = max(m, (int)(s_misc[3] + s_misc[2]));
+    }
+  }
+  if (zt.child) {
+    // Clear the octree tags of those slots (the intervals of consecutive tiles
+    // meet, so all of [0, M) is cleared before stages 7-8 run).
+    __syncthreads();
+    const int lo = (int)s_misc[3];
+    const int hi = min(s_hi, zt.cap - 1);
+    uint4* c4 = reinterpret_cast<uint4*>(zt.child);
+    for (int p = lo + tid; p <= hi; p += kEsThreads) {
+      c4[2 * p] = make_uint4(0, 0, 0, 0);
+      c4[2 * p + 1] = make_uint4(0, 0, 0, 0);
+      zt.owner[p] = 0;
+      zt.mask[p] = 0;
     }
   }
   (void)tiles;
@@ -331,7 +353,44 @@ cudaError_t launch_edge_scan(int mode, int n_host, const int* d_unique, const ui
   uint32_t* counter = c ? reinterpret_cast<uint32_t*>(c + plan->counter_off) : nullptr;
   if (mode != kEdgeOnly && !c) return cudaErrorInvalidValue;
   edge_scan_kernel<<<plan->tiles, kEsThreads, 0, s>>>(mode, n_host, d_unique, prefix_n, parent,
-                                                      ec, ps, d_max_slot, lb, counter, status);
+                                                      ec, ps, d_max_slot, lb, counter, status,
+                                                      OctTags{}, nullptr);
+  return cudaGetLastError();
+}
+
+// Exclusive scan of the per-tile edge-count sums (one CTA).
+constexpr int kTsThreads = 1024;
+__global__ void __launch_bounds__(kTsThreads)
+    tile_sums_scan_kernel(int n_host, const int* __restrict__ d_unique,
+                          const int* __restrict__ tile_sum, uint32_t* __restrict__ tile_prefix) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
+  const int tiles = (n + kEsTile - 1) / kEsTile;
+  const int per = (tiles + kTsThreads - 1) / kTsThreads;
+  const int j0 = threadIdx.x * per;
+  uint32_t sum = 0;
+  for (int j = j0; j < min(j0 + per, tiles); ++j) sum += (uint32_t)tile_sum[j];
+  uint32_t run = block_exclusive_sum<kTsThreads>(sum, s_warp, &s_total);
+  for (int j = j0; j < min(j0 + per, tiles); ++j) {
+    tile_prefix[j] = run;
+    run += (uint32_t)tile_sum[j];
+  }
+}
+
+cudaError_t launch_prefix_sum_clear_tags(int n_host, const int* d_unique, int* ec, int* ps,
+                                         int* d_max_slot, void* tree_scratch, uint32_t* status,
+                                         const OctTags& tags, cudaStream_t s) {
+  static_assert(kEsTile == 4096, "scan tiles are the radix-tree tiles");
+  if (n_host <= 0) return cudaSuccess;
+  const TreeScratch S = tree_scratch_carve(tree_scratch, n_host);
+  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(n_host, d_unique, S.tile_sum, S.tile_prefix);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int tiles = (n_host + kEsTile - 1) / kEsTile;
+  edge_scan_kernel<<<tiles, kEsThreads, 0, s>>>(kScanOnly, n_host, d_unique, nullptr, nullptr, ec,
+                                                ps, d_max_slot, nullptr, nullptr, status,
+                                                tags.cap > 0 ? tags : OctTags{}, S.tile_prefix);
   return cudaGetLastError();
 }
 

@@ -53,7 +53,7 @@ static int tt_tiles(int n) { return ((n > 1 ? n : 1) + kTtTile - 1) / kTtTile; }
 size_t tree_scratch_bytes(int n) {
   const size_t t = (size_t)tt_tiles(n);
   return align_up(t * kTtTile, 256) + 2 * align_up(t * 32 * sizeof(int), 256) +
-         align_up(align_up(t, kTtMinBlock), 256);
+         align_up(align_up(t, kTtMinBlock), 256) + 2 * align_up(t * sizeof(int), 256);
 }
 
 TreeScratch tree_scratch_carve(void* base, int n) {
@@ -68,6 +68,10 @@ TreeScratch tree_scratch_carve(void* base, int n) {
   S.tile_first = reinterpret_cast<int*>(p);
   p += align_up(t * 32 * sizeof(int), 256);
   S.tile_min = reinterpret_cast<uint8_t*>(p);
+  p += align_up(align_up(t, kTtMinBlock), 256);
+  S.tile_sum = reinterpret_cast<int*>(p);
+  p += align_up(t * sizeof(int), 256);
+  S.tile_prefix = reinterpret_cast<uint32_t*>(p);
   return S;
 }
 
@@ -162,7 +166,10 @@ __global__ void __launch_bounds__(kTtAThreads)
     }
     S.tile_last[t * 32 + lane] = l;
     S.tile_first[t * 32 + lane] = f;
-    if (lane == 0) S.tile_min[t] = (uint8_t)m;
+    if (lane == 0) {
+      S.tile_min[t] = (uint8_t)m;
+      S.tile_sum[t] = 0;
+    }
   }
 }
 
@@ -310,6 +317,7 @@ __global__ void __launch_bounds__(kTtBThreads)
   }
   __syncwarp();
 
+  int own_sum = 0;  // edge counts of this tile's nodes emitted here
 #pragma unroll 1
   for (int k = 0; k < kTtChunksPerWarp; ++k) {
     const int c = warp * kTtChunksPerWarp + k;
@@ -368,8 +376,18 @@ __global__ void __launch_bounds__(kTtBThreads)
     o.hlr[i] = lr;
     if (!ll) o.parent[q] = i;
     if (!lr) o.parent[q + 1] = i;
-    if (o.ec) o.ec[i] = short_root ? 0 : (int)(xv / 3) - max(da, db) / 3;
+    if (o.ec) {
+      const int e = short_root ? 0 : (int)(xv / 3) - max(da, db) / 3;
+      o.ec[i] = e;
+      if ((i / kTtTile) == t) own_sum += e;
+      else atomicAdd(S.tile_sum + i / kTtTile, e);
+    }
     if (short_root) emit_root(o, n, q, xv, true);
+  }
+  if (o.ec) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) own_sum += __shfl_xor_sync(kFull, own_sum, off);
+    if (lane == 0 && own_sum != 0) atomicAdd(S.tile_sum + t, own_sum);
   }
 }
 
