@@ -11,10 +11,15 @@
 //   sort      reduce-then-scan radix passes: per-tile digit histograms, a
 //             per-cloud tile-prefix scan, and the pass kernel driven by tile
 //             descriptors (cloud-local positions are absolute indices);
-//   unique,   decoupled look-back chains that restart at each cloud's first
-//   scan      tile; tiles come from an atomic work queue;
-//   tree,     one thread per global node / slot, mapped to its cloud by a
-//   octree    binary search over the cloud starts, reusing the single-cloud
+//   unique    decoupled look-back chains that restart at each cloud's first
+//             tile; tiles come from an atomic work queue;
+//   tree      the single-cloud delta kernels over the same 4,096-position
+//             tiles (tile map: cloud, cloud start, the cloud's tile range),
+//             writing the edge counts and their per-tile sums;
+//   scan      one scan of the tile sums for all clouds; a tile's prefix is its
+//             entry minus that of its cloud's first tile, so no tile waits;
+//   octree    one thread per global node / slot, mapped to its cloud by a
+//             binary search over the cloud starts, reusing the single-cloud
 //             node and slot functions on per-cloud views.
 //
 // The host plan (tile descriptors, cloud starts) is uploaded once; every
@@ -268,99 +273,54 @@ __global__ void __launch_bounds__(kBuThreads)
   }
 }
 
-// ------------------------------------------------------------ radix tree --
+// ------------------------------------------------------------ prefix sum --
+// Inclusive prefix sum of each cloud's edge counts (written by the tree
+// kernels with their per-tile sums, scanned into tile_prefix), and each
+// cloud's largest octree slot.
 __global__ void __launch_bounds__(256)
-    batch_tree_kernel(const uint32_t* __restrict__ codes, BatchDev B,
-                      const int* __restrict__ unique_c, uint8_t* __restrict__ prefix_n,
-                      uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
-                      int* __restrict__ left_child, int* __restrict__ parent) {
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < B.N; g += gridDim.x * blockDim.x) {
-    const int c = cloud_of(B.start, B.C, g);
-    const int cs = B.start[c];
-    const int nb = max(unique_c[c] - 1, 0);
-    const int i = g - cs;
-    if (i < nb)
-      radix_node(i, nb, GlobalCodes{codes + cs}, prefix_n + cs, hll + cs, hlr + cs,
-                 left_child + cs, parent + cs);
-  }
-}
-
-// ------------------------------------------------- edge count + prefix sum --
-__global__ void __launch_bounds__(256)
-    batch_edge_scan_kernel(BatchDev B, const int* __restrict__ unique_c,
-                           const uint8_t* __restrict__ prefix_n, const int* __restrict__ parent,
-                           int* __restrict__ ec_out, int* __restrict__ ps_out,
-                           int* __restrict__ max_slot_c, unsigned long long* __restrict__ lb,
-                           uint32_t* __restrict__ queue, uint32_t* __restrict__ status) {
+    batch_prefix_sum_kernel(BatchDev B, const int* __restrict__ unique_c,
+                            const int* __restrict__ ec, int* __restrict__ ps_out,
+                            int* __restrict__ max_slot_c, const uint32_t* __restrict__ tile_prefix) {
   __shared__ uint32_t s_warp[32];
-  __shared__ uint32_t s_misc[4];
+  __shared__ uint32_t s_total;
   __shared__ int s_max[8];
   const int tid = threadIdx.x;
   constexpr int ITEMS = 16;
-  while (true) {
-    if (tid == 0) s_misc[0] = atomicAdd(queue, 1u);
-    __syncthreads();
-    const int t = (int)s_misc[0];
-    if (t >= B.T4) return;
-    const int4 d = B.tiles4k[t];
-    const int c = d.z, cs = B.start[c];
-    const int n = max(unique_c[c] - 1, 0);  // radix nodes of this cloud
-    const int lo = d.x - cs;                // first node of the tile (cloud-local)
-    if (lo >= n) {                          // past this cloud's nodes: nobody waits on it
-      __syncthreads();
-      continue;
-    }
-    const uint8_t* pn = prefix_n + cs;
-    const int* par = parent + cs;
-    const int j0 = lo + tid * ITEMS;
-    int v[ITEMS];
+  const int t = blockIdx.x;
+  const int4 d = B.tiles4k[t];
+  const int c = d.z, cs = B.start[c];
+  const int n = max(unique_c[c] - 1, 0);  // radix nodes of this cloud
+  const int lo = d.x - cs;                // first node of the tile (cloud-local)
+  if (lo >= n) return;
+  const int j0 = lo + tid * ITEMS;
+  int v[ITEMS];
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const int i = j0 + k;
-      int e = 0;
-      if (i > 0 && i < n) {
-        int p = par[i];
-        if ((unsigned)p >= (unsigned)n) {
-          raise_status(status, kStatusWalkLimit);
-          p = 0;
-        }
-        e = (int)(pn[i] / 3) - (int)(pn[p] / 3);
-      }
-      v[k] = e;
-    }
-    uint32_t sum = 0;
+  for (int k = 0; k < ITEMS; ++k) v[k] = j0 + k < n ? ec[cs + j0 + k] : 0;
+  uint32_t sum = 0;
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) sum += (uint32_t)v[k];
-    const uint32_t off = block_exclusive_sum<256>(sum, s_warp, &s_misc[2]);
-    if (tid < 32) {
-      const uint32_t e = chain_lookback(lb, t, d.w, s_misc[2], status);
-      if (tid == 0) s_misc[3] = e;
-    }
-    __syncthreads();
-    uint32_t run = s_misc[3] + off;
-    int mx = 0;
+  for (int k = 0; k < ITEMS; ++k) sum += (uint32_t)v[k];
+  const uint32_t off = block_exclusive_sum<256>(sum, s_warp, &s_total);
+  uint32_t run = tile_prefix[t] - tile_prefix[d.w] + off;
+  int mx = 0;
 #pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const int i = j0 + k;
-      run += (uint32_t)v[k];
-      if (i < n) {
-        ec_out[cs + i] = v[k];
-        ps_out[cs + i] = (int)run;
-        const int last = v[k] > 0 ? (int)run + v[k] - 1 : (int)run;
-        if (i > 0 && v[k] > 0 && last > mx) mx = last;
-        if (i == n - 1 && (int)run > mx) mx = (int)run;
-      }
+  for (int k = 0; k < ITEMS; ++k) {
+    const int i = j0 + k;
+    run += (uint32_t)v[k];
+    if (i < n) {
+      ps_out[cs + i] = (int)run;
+      const int last = v[k] > 0 ? (int)run + v[k] - 1 : (int)run;
+      if (i > 0 && v[k] > 0 && last > mx) mx = last;
+      if (i == n - 1 && (int)run > mx) mx = (int)run;
     }
+  }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((tid & 31) == 0) s_max[tid >> 5] = mx;
-    __syncthreads();
-    if (tid == 0) {
-      int m = 0;
-      for (int w = 0; w < 8; ++w) m = max(m, s_max[w]);
-      atomicMax(&max_slot_c[c], m);
-    }
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((tid & 31) == 0) s_max[tid >> 5] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    int m = 0;
+    for (int w = 0; w < 8; ++w) m = max(m, s_max[w]);
+    atomicMax(&max_slot_c[c], m);
   }
 }
 
@@ -516,7 +476,7 @@ struct oct_batch_plan {
   size_t t_start = 0, t_node_start = 0, t_tile0 = 0, t_sort = 0, t_4k = 0, tables_bytes = 0;
   // workspace offsets
   size_t w_status = 0, w_unique = 0, w_maxslot = 0, w_hist = 0, w_queues = 0, w_lb_u = 0,
-         w_lb_s = 0, zero_bytes = 0, w_base = 0, w_th = 0, w_keys_a = 0, w_keys_b = 0,
+         zero_bytes = 0, w_tree = 0, w_base = 0, w_th = 0, w_keys_a = 0, w_keys_b = 0,
          w_tags = 0, ws_bytes = 0;
 };
 
@@ -615,8 +575,8 @@ OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_siz
   P->w_hist = take(4 * (size_t)n_clouds * passes * bins);
   P->w_queues = take(64);
   P->w_lb_u = take(8 * (P->tiles4k.size() + 1));
-  P->w_lb_s = take(8 * (P->tiles4k.size() + 1));
   P->zero_bytes = o;
+  P->w_tree = take(tree_scratch_bytes_tiles((int)P->tiles4k.size()));
   P->w_base = take(4 * (size_t)n_clouds * passes * bins);
   P->w_th = take(4 * (P->sort_tiles.size() + 1) * bins);
   P->w_keys_a = take(4 * (size_t)std::max(P->N, 1));
@@ -686,7 +646,6 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
   uint32_t* hist = reinterpret_cast<uint32_t*>(w + P->w_hist);
   uint32_t* queues = reinterpret_cast<uint32_t*>(w + P->w_queues);
   unsigned long long* lb_u = reinterpret_cast<unsigned long long*>(w + P->w_lb_u);
-  unsigned long long* lb_s = reinterpret_cast<unsigned long long*>(w + P->w_lb_s);
   uint32_t* base = reinterpret_cast<uint32_t*>(w + P->w_base);
   uint32_t* th = reinterpret_cast<uint32_t*>(w + P->w_th);
   uint32_t* ka = reinterpret_cast<uint32_t*>(w + P->w_keys_a);
@@ -727,12 +686,16 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
     batch_unique_kernel<<<qgrid, kBuThreads, 0, s>>>(a, out->codes, B, unique_c, lb_u, queues,
                                                      status);
     const int ngrid = std::max(1, std::min((P->N + 255) / 256, sms * 16));
-    batch_tree_kernel<<<ngrid, 256, 0, s>>>(out->codes, B, unique_c, out->tree.prefix_n,
-                                            out->tree.has_leaf_left, out->tree.has_leaf_right,
-                                            out->tree.left_child, out->tree.parent);
-    batch_edge_scan_kernel<<<qgrid, 256, 0, s>>>(B, unique_c, out->tree.prefix_n, out->tree.parent,
-                                                 out->edge_count, out->prefix_sum, max_slot_c,
-                                                 lb_s, queues + 1, status);
+    void* tree_ws = w + P->w_tree;
+    const TreeScratch TS = tree_scratch_carve_tiles(tree_ws, B.T4);
+    e = launch_batch_radix_tree(B.tiles4k, B.T4, B.start, unique_c, out->codes,
+                                out->tree.prefix_n, out->tree.has_leaf_left,
+                                out->tree.has_leaf_right, out->tree.left_child, out->tree.parent,
+                                out->edge_count, tree_ws, s);
+    if (e == cudaSuccess) e = launch_tile_sums_scan(B.T4, TS.tile_sum, TS.tile_prefix, s);
+    if (e != cudaSuccess) return batch_fail(e, "batch: tree");
+    batch_prefix_sum_kernel<<<B.T4, 256, 0, s>>>(B, unique_c, out->edge_count, out->prefix_sum,
+                                                 max_slot_c, TS.tile_prefix);
     BatchOctDev O;
     O.nodes = out->nodes;
     O.offsets = out->prefix_sum;

@@ -123,6 +123,14 @@ struct TreeScratch {
 };
 size_t tree_scratch_bytes(int n_host);
 TreeScratch tree_scratch_carve(void* base, int n_host);
+size_t tree_scratch_bytes_tiles(int tiles);
+TreeScratch tree_scratch_carve_tiles(void* base, int tiles);
+// Batched clouds: tiles {first, end, cloud, first tile of cloud} of 4,096
+// positions that never cross clouds; start[C+1]; U per cloud on the device.
+cudaError_t launch_batch_radix_tree(const int4* tiles, int n_tiles, const int* start,
+                                    const int* unique_c, const uint32_t* codes, uint8_t* prefix_n,
+                                    uint8_t* hll, uint8_t* hlr, int* left_child, int* parent,
+                                    int* ec, void* scratch, cudaStream_t s);
 cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint32_t* codes,
                                      uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
                                      int* left_child, int* parent, int* ec, void* scratch,
@@ -175,6 +183,10 @@ cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t
 // clears the octree tags of every slot stages 7-8 can touch, up to the tags'
 // capacity: one small kernel scans the tile sums, then every tile scans its
 // own nodes from its prefix (no inter-tile waits).
+// Exclusive scan of tiles per-tile sums (one CTA).
+cudaError_t launch_tile_sums_scan(int tiles, const int* tile_sum, uint32_t* tile_prefix,
+                                  cudaStream_t s);
+
 cudaError_t launch_prefix_sum_clear_tags(int n_host, const int* d_unique, int* ec, int* ps,
                                          int* d_max_slot, void* tree_scratch, uint32_t* status,
                                          const OctTags& tags, cudaStream_t s);

@@ -361,12 +361,12 @@ cudaError_t launch_edge_scan(int mode, int n_host, const int* d_unique, const ui
 // Exclusive scan of the per-tile edge-count sums (one CTA).
 constexpr int kTsThreads = 1024;
 __global__ void __launch_bounds__(kTsThreads)
-    tile_sums_scan_kernel(int n_host, const int* __restrict__ d_unique,
+    tile_sums_scan_kernel(int tiles_fixed, int n_host, const int* __restrict__ d_unique,
                           const int* __restrict__ tile_sum, uint32_t* __restrict__ tile_prefix) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
-  const int tiles = (n + kEsTile - 1) / kEsTile;
+  const int tiles = tiles_fixed > 0 ? tiles_fixed : (n + kEsTile - 1) / kEsTile;
   const int per = (tiles + kTsThreads - 1) / kTsThreads;
   const int j0 = threadIdx.x * per;
   uint32_t sum = 0;
@@ -384,7 +384,7 @@ cudaError_t launch_prefix_sum_clear_tags(int n_host, const int* d_unique, int* e
   static_assert(kEsTile == 4096, "scan tiles are the radix-tree tiles");
   if (n_host <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve(tree_scratch, n_host);
-  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(n_host, d_unique, S.tile_sum, S.tile_prefix);
+  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(0, n_host, d_unique, S.tile_sum, S.tile_prefix);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int tiles = (n_host + kEsTile - 1) / kEsTile;
@@ -413,6 +413,13 @@ cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* c
   const int grid = (n_host + 255) / 256;
   radix_tree_kernel<<<grid, 256, 0, s>>>(n_host, d_unique, codes, prefix_n, hll, hlr,
                                          left_child, parent);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_sums_scan(int tiles, const int* tile_sum, uint32_t* tile_prefix,
+                                  cudaStream_t s) {
+  if (tiles <= 0) return cudaSuccess;
+  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(tiles, 0, nullptr, tile_sum, tile_prefix);
   return cudaGetLastError();
 }
 

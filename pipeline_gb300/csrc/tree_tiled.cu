@@ -50,14 +50,14 @@ constexpr uint32_t kFull = 0xffffffffu;
 
 static int tt_tiles(int n) { return ((n > 1 ? n : 1) + kTtTile - 1) / kTtTile; }
 
-size_t tree_scratch_bytes(int n) {
-  const size_t t = (size_t)tt_tiles(n);
+size_t tree_scratch_bytes_tiles(int tiles) {
+  const size_t t = (size_t)(tiles > 1 ? tiles : 1);
   return align_up(t * kTtTile, 256) + 2 * align_up(t * 32 * sizeof(int), 256) +
          align_up(align_up(t, kTtMinBlock), 256) + 2 * align_up(t * sizeof(int), 256);
 }
 
-TreeScratch tree_scratch_carve(void* base, int n) {
-  const size_t t = (size_t)tt_tiles(n);
+TreeScratch tree_scratch_carve_tiles(void* base, int tiles) {
+  const size_t t = (size_t)(tiles > 1 ? tiles : 1);
   char* p = static_cast<char*>(base);
   TreeScratch S;
   S.tiles = (int)t;
@@ -73,6 +73,61 @@ TreeScratch tree_scratch_carve(void* base, int n) {
   p += align_up(t * sizeof(int), 256);
   S.tile_prefix = reinterpret_cast<uint32_t*>(p);
   return S;
+}
+
+size_t tree_scratch_bytes(int n) { return tree_scratch_bytes_tiles(tt_tiles(n)); }
+TreeScratch tree_scratch_carve(void* base, int n) { return tree_scratch_carve_tiles(base, tt_tiles(n)); }
+
+// Where a tile sits: tiles never cross clouds, and a cloud's tiles start at
+// its first position and cover 4,096 positions each; positions are
+// cloud-local, arrays are indexed from the cloud's start cs.
+struct TileInfo {
+  int t;        // tile
+  int t_first;  // first and last tile of its cloud
+  int t_last;
+  int n;        // radix nodes of the cloud
+  int lo;       // first position of the tile
+  int cs;       // cloud start in the concatenated arrays
+};
+
+// One cloud: tile t covers positions [4096 t, 4096 t + 4096).
+struct OneCloud {
+  int n_host;
+  const int* d_unique;
+  int tiles;
+  __device__ __forceinline__ TileInfo operator()(int t) const {
+    TileInfo I;
+    I.t = t;
+    I.t_first = 0;
+    I.t_last = tiles - 1;
+    I.n = d_unique ? max(*d_unique - 1, 0) : n_host;
+    I.lo = t * kTtTile;
+    I.cs = 0;
+    return I;
+  }
+};
+
+// Batched clouds: tile descriptors {first, end, cloud, first tile of cloud}.
+struct CloudTiles {
+  const int4* tiles;
+  const int* start;
+  const int* unique_c;
+  __device__ __forceinline__ TileInfo operator()(int t) const {
+    const int4 d = tiles[t];
+    TileInfo I;
+    I.t = t;
+    I.cs = start[d.z];
+    I.t_first = d.w;
+    I.t_last = d.w + (start[d.z + 1] - I.cs + kTtTile - 1) / kTtTile - 1;
+    I.n = max(unique_c[d.z] - 1, 0);
+    I.lo = d.x - I.cs;
+    return I;
+  }
+};
+
+// Delta of cloud position p in the tile-major delta array.
+__device__ __forceinline__ size_t d_index(const TileInfo& I, int p) {
+  return (size_t)(I.t_first + p / kTtTile) * kTtTile + (size_t)(p % kTtTile);
 }
 
 // Lanes whose 5-bit value is below v, from the ballots b[k] of the values'
@@ -101,15 +156,16 @@ __device__ __forceinline__ uint32_t tt_delta(uint32_t a, uint32_t b) {
   return min((uint32_t)delta_u8(a, b), kTtAbsent);
 }
 
+template <class Map>
 __global__ void __launch_bounds__(kTtAThreads)
-    tree_tiles_kernel(int n_host, const int* __restrict__ d_unique,
-                      const uint32_t* __restrict__ codes, TreeScratch S) {
+    tree_tiles_kernel(Map map, const uint32_t* __restrict__ codes_all, TreeScratch S) {
   constexpr int kWarps = kTtAThreads / 32;
   __shared__ int s_last[kWarps][32], s_first[kWarps][32];
   __shared__ uint32_t s_min[kWarps];
-  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
-  const int t = blockIdx.x;
-  const int t0 = t * kTtTile;
+  const TileInfo I = map(blockIdx.x);
+  const int n = I.n, t = I.t, t0 = I.lo;
+  const uint32_t* codes = codes_all + I.cs;
+  uint8_t* Dt = S.D + (size_t)t * kTtTile;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (t == 0) {  // whole blocks of the tile-minimum array; the padding never matches
     const int pad = (int)align_up((size_t)S.tiles, kTtMinBlock);
@@ -137,7 +193,7 @@ __global__ void __launch_bounds__(kTtAThreads)
         uint32_t cn = __shfl_down_sync(kFull, cp[j], 1);
         if (lane == 31) cn = cx[j];
         const uint32_t d = p < n ? tt_delta(cp[j], cn) : kTtAbsent;
-        S.D[p] = (uint8_t)d;
+        Dt[32 * c + lane] = (uint8_t)d;
         dmin = min(dmin, d);
         uint32_t b[5];
         value_ballots(d, b);
@@ -183,15 +239,17 @@ __device__ __forceinline__ uint32_t bytes_below(const uint4& w, uint32_t x) {
   return m;
 }
 
-// Largest tile <= hi whose smallest delta is below x, or -1 (whole warp).
-__device__ int tiles_scan_left(const uint8_t* __restrict__ tmin, int hi, uint32_t x, int lane) {
-  if (hi < 0) return -1;
-  for (int blk = hi / kTtMinBlock; blk >= 0; --blk) {
+// Largest tile in [lo, hi] whose smallest delta is below x, or -1 (whole warp).
+__device__ int tiles_scan_left(const uint8_t* __restrict__ tmin, int lo, int hi, uint32_t x,
+                               int lane) {
+  if (hi < lo) return -1;
+  for (int blk = hi / kTtMinBlock; blk >= lo / kTtMinBlock; --blk) {
     const uint4 w = reinterpret_cast<const uint4*>(tmin + (size_t)blk * kTtMinBlock)[lane];
     uint32_t m = bytes_below(w, x);
     const int base = blk * kTtMinBlock + lane * 16;
-    if (base > hi) m = 0;
-    else if (base + 15 > hi) m &= (2u << (hi - base)) - 1u;
+    if (base > hi || base + 15 < lo) m = 0;
+    if (base + 15 > hi && base <= hi) m &= (2u << (hi - base)) - 1u;
+    if (base < lo && base + 15 >= lo) m &= ~((1u << (lo - base)) - 1u);
     const uint32_t any = __ballot_sync(kFull, m != 0);
     if (any) {
       const int L = 31 - __clz(any);
@@ -202,16 +260,17 @@ __device__ int tiles_scan_left(const uint8_t* __restrict__ tmin, int hi, uint32_
   return -1;
 }
 
-// Smallest tile >= lo whose smallest delta is below x, or -1 (whole warp).
-__device__ int tiles_scan_right(const uint8_t* __restrict__ tmin, int lo, int tiles, uint32_t x,
+// Smallest tile in [lo, hi] whose smallest delta is below x, or -1 (whole warp).
+__device__ int tiles_scan_right(const uint8_t* __restrict__ tmin, int lo, int hi, uint32_t x,
                                 int lane) {
-  const int blocks = (tiles + kTtMinBlock - 1) / kTtMinBlock;
-  for (int blk = lo / kTtMinBlock; blk < blocks; ++blk) {
+  if (hi < lo) return -1;
+  for (int blk = lo / kTtMinBlock; blk <= hi / kTtMinBlock; ++blk) {
     const uint4 w = reinterpret_cast<const uint4*>(tmin + (size_t)blk * kTtMinBlock)[lane];
     uint32_t m = bytes_below(w, x);
     const int base = blk * kTtMinBlock + lane * 16;
-    if (base + 15 < lo) m = 0;
-    else if (base < lo) m &= ~((1u << (lo - base)) - 1u);
+    if (base > hi || base + 15 < lo) m = 0;
+    if (base + 15 > hi && base <= hi) m &= (2u << (hi - base)) - 1u;
+    if (base < lo && base + 15 >= lo) m &= ~((1u << (lo - base)) - 1u);
     const uint32_t any = __ballot_sync(kFull, m != 0);
     if (any) {
       const int L = __ffs(any) - 1;
@@ -248,18 +307,25 @@ __device__ __forceinline__ void emit_root(const TreeOut& o, int n, int q, uint32
   if (o.ec) o.ec[0] = 0;
 }
 
+template <class Map>
 __global__ void __launch_bounds__(kTtBThreads)
-    tree_nodes_kernel(int n_host, const int* __restrict__ d_unique,
-                      const uint32_t* __restrict__ codes, TreeScratch S, TreeOut o) {
+    tree_nodes_kernel(Map map, const uint32_t* __restrict__ codes, TreeScratch S, TreeOut o) {
   __shared__ __align__(16) uint8_t s_D[kTtTile];
   __shared__ int16_t s_pl[kTtChunks][32];  // last tile position before the chunk with D < v
   __shared__ int16_t s_sf[kTtChunks][32];  // first tile position after the chunk with D < v
   __shared__ int16_t s_wl[kTtBWarps][32], s_wf[kTtBWarps][32];
   __shared__ uint8_t s_pv[kTtTile], s_nv[kTtTile];  // nearest smaller lane in the chunk, or 0xFF
-  const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
-  const int t = blockIdx.x;
-  const int t0 = t * kTtTile;
+  const TileInfo I = map(blockIdx.x);
+  const int n = I.n, t = I.t, t0 = I.lo;
   if (t0 >= n) return;
+  // the cloud's arrays
+  codes += I.cs;
+  o.prefix_n += I.cs;
+  o.hll += I.cs;
+  o.hlr += I.cs;
+  o.left_child += I.cs;
+  o.parent += I.cs;
+  if (o.ec) o.ec += I.cs;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (n < 2) {  // a single node: the reference's search steps
     if (tid == 0) {
@@ -269,7 +335,8 @@ __global__ void __launch_bounds__(kTtBThreads)
     return;
   }
   if (tid < kTtTile / 16)
-    reinterpret_cast<uint4*>(s_D)[tid] = reinterpret_cast<const uint4*>(S.D + t0)[tid];
+    reinterpret_cast<uint4*>(s_D)[tid] =
+        reinterpret_cast<const uint4*>(S.D + (size_t)t * kTtTile)[tid];
   __syncthreads();
 
   const uint32_t below_me = (1u << lane) - 1u;
@@ -333,11 +400,11 @@ __global__ void __launch_bounds__(kTtBThreads)
       if (nv != 0xFF) b = t0 + 32 * c + (int)nv;
       else if (s_sf[c][xv] < kTtTile) b = t0 + s_sf[c][xv];
       if (a == -2) {  // the previous tile first
-        if (t == 0) a = -1;
+        if (t == I.t_first) a = -1;
         else if (S.tile_last[(t - 1) * 32 + xv] >= 0) a = S.tile_last[(t - 1) * 32 + xv];
       }
       if (b == -2) {
-        if (t + 1 >= S.tiles) b = n;
+        if (t + 1 > I.t_last) b = n;
         else if (S.tile_first[(t + 1) * 32 + xv] != INT_MAX) b = S.tile_first[(t + 1) * 32 + xv];
       }
     }
@@ -347,7 +414,7 @@ __global__ void __launch_bounds__(kTtBThreads)
       const int src = __ffs(need) - 1;
       need &= need - 1;
       const uint32_t qx = __shfl_sync(kFull, xv, src);
-      const int tt = tiles_scan_left(S.tile_min, t - 2, qx, lane);
+      const int tt = tiles_scan_left(S.tile_min, I.t_first, t - 2, qx, lane);
       const int ans = tt >= 0 ? S.tile_last[tt * 32 + qx] : -1;
       if (lane == src) a = ans;
     }
@@ -356,13 +423,13 @@ __global__ void __launch_bounds__(kTtBThreads)
       const int src = __ffs(need) - 1;
       need &= need - 1;
       const uint32_t qx = __shfl_sync(kFull, xv, src);
-      const int tt = tiles_scan_right(S.tile_min, t + 2, S.tiles, qx, lane);
+      const int tt = tiles_scan_right(S.tile_min, t + 2, I.t_last, qx, lane);
       const int ans = tt >= 0 ? S.tile_first[tt * 32 + qx] : n;
       if (lane == src) b = ans;
     }
     if (!live) continue;
-    const int da = a < 0 ? -1 : (a >= t0 ? (int)s_D[a - t0] : (int)S.D[a]);
-    const int db = b >= n ? -1 : (b < t0 + kTtTile ? (int)s_D[b - t0] : (int)S.D[b]);
+    const int da = a < 0 ? -1 : (a >= t0 ? (int)s_D[a - t0] : (int)S.D[d_index(I, a)]);
+    const int db = b >= n ? -1 : (b < t0 + kTtTile ? (int)s_D[b - t0] : (int)S.D[d_index(I, b)]);
     if (a < 0 && b >= n) {  // the smallest delta overall
       if (q <= n - 2) emit_root(o, n, q, xv, false);
       continue;             // at n - 1: the root is short; node 0 comes from [0, n - 2]'s split
@@ -379,8 +446,9 @@ __global__ void __launch_bounds__(kTtBThreads)
     if (o.ec) {
       const int e = short_root ? 0 : (int)(xv / 3) - max(da, db) / 3;
       o.ec[i] = e;
-      if ((i / kTtTile) == t) own_sum += e;
-      else atomicAdd(S.tile_sum + i / kTtTile, e);
+      const int ti = I.t_first + i / kTtTile;
+      if (ti == t) own_sum += e;
+      else atomicAdd(S.tile_sum + ti, e);
     }
     if (short_root) emit_root(o, n, q, xv, true);
   }
@@ -397,11 +465,27 @@ cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint
                                      cudaStream_t s) {
   if (n_host <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve(scratch, n_host);
-  tree_tiles_kernel<<<S.tiles, kTtAThreads, 0, s>>>(n_host, d_unique, codes, S);
+  const OneCloud map{n_host, d_unique, S.tiles};
+  tree_tiles_kernel<<<S.tiles, kTtAThreads, 0, s>>>(map, codes, S);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
-  tree_nodes_kernel<<<S.tiles, kTtBThreads, 0, s>>>(n_host, d_unique, codes, S, o);
+  tree_nodes_kernel<<<S.tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_radix_tree(const int4* tiles, int n_tiles, const int* start,
+                                    const int* unique_c, const uint32_t* codes, uint8_t* prefix_n,
+                                    uint8_t* hll, uint8_t* hlr, int* left_child, int* parent,
+                                    int* ec, void* scratch, cudaStream_t s) {
+  if (n_tiles <= 0) return cudaSuccess;
+  const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
+  const CloudTiles map{tiles, start, unique_c};
+  tree_tiles_kernel<<<n_tiles, kTtAThreads, 0, s>>>(map, codes, S);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
+  tree_nodes_kernel<<<n_tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
   return cudaGetLastError();
 }
 
