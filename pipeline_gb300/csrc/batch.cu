@@ -18,9 +18,10 @@
 //             writing the edge counts and their per-tile sums;
 //   scan      one scan of the tile sums for all clouds; a tile's prefix is its
 //             entry minus that of its cloud's first tile, so no tile waits;
-//   octree    one thread per global node / slot, mapped to its cloud by a
-//             binary search over the cloud starts, reusing the single-cloud
-//             node and slot functions on per-cloud views.
+//   octree    the tags are cleared by the prefix-sum tiles; then one CTA per
+//             4,096-node tile (emit) and per 256-slot tile (finalize) of a
+//             cloud, reusing the single-cloud node and slot functions on
+//             per-cloud views.
 //
 // The host plan (tile descriptors, cloud starts) is uploaded once; every
 // size that depends on the data (U_c, M_c) stays on the device, so a batch
@@ -61,6 +62,8 @@ struct BatchDev {
   const int* cloud_tile0; // [C+1] first sort tile of each cloud
   const int4* tiles4k;    // [T4] {first, end, cloud, first tile of cloud}
   int T4;
+  const int4* slot_tiles; // [Tn] {first slot, end slot, cloud, 0}: 256 OctNode slots
+  int Tn;
 };
 
 // ------------------------------------------------------------------ morton --
@@ -280,10 +283,12 @@ __global__ void __launch_bounds__(kBuThreads)
 __global__ void __launch_bounds__(256)
     batch_prefix_sum_kernel(BatchDev B, const int* __restrict__ unique_c,
                             const int* __restrict__ ec, int* __restrict__ ps_out,
-                            int* __restrict__ max_slot_c, const uint32_t* __restrict__ tile_prefix) {
+                            int* __restrict__ max_slot_c, const uint32_t* __restrict__ tile_prefix,
+                            OctTags tags) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ int s_max[8];
+  __shared__ int s_hi;
   const int tid = threadIdx.x;
   constexpr int ITEMS = 16;
   const int t = blockIdx.x;
@@ -300,7 +305,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) sum += (uint32_t)v[k];
   const uint32_t off = block_exclusive_sum<256>(sum, s_warp, &s_total);
-  uint32_t run = tile_prefix[t] - tile_prefix[d.w] + off;
+  const uint32_t ex = tile_prefix[t] - tile_prefix[d.w];
+  uint32_t run = ex + off;
   int mx = 0;
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
@@ -321,6 +327,21 @@ __global__ void __launch_bounds__(256)
     int m = 0;
     for (int w = 0; w < 8; ++w) m = max(m, s_max[w]);
     atomicMax(&max_slot_c[c], m);
+    s_hi = max(m, (int)(ex + s_total));
+  }
+  // Clear the cloud's octree tags of the tile's slots: from the tile's
+  // exclusive prefix to its largest slot or last prefix (consecutive tiles'
+  // intervals meet, so [0, M_c) is cleared before stages 7-8 run).
+  __syncthreads();
+  const int ns = B.node_start[c];
+  const int hi = min(s_hi, B.node_start[c + 1] - ns - 1);
+  uint4* c4 = reinterpret_cast<uint4*>(tags.child);
+  for (int p = (int)ex + tid; p <= hi; p += 256) {
+    const size_t g = (size_t)ns + p;
+    c4[2 * g] = make_uint4(0, 0, 0, 0);
+    c4[2 * g + 1] = make_uint4(0, 0, 0, 0);
+    tags.owner[g] = 0;
+    tags.mask[g] = 0;
   }
 }
 
@@ -386,69 +407,54 @@ __device__ __forceinline__ OctTags cloud_tags(const BatchOctDev& O, const CloudS
   return t;
 }
 
-__global__ void __launch_bounds__(256)
-    batch_oct_zero_kernel(BatchDev B, BatchOctDev O, int total_cap, uint32_t* __restrict__ status) {
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total_cap; g += gridDim.x * blockDim.x) {
-    const int c = cloud_of(B.node_start, B.C, g);
-    const CloudSizes z = cloud_sizes(B, O, c);
-    const int p = g - z.ns;
-    if (!z.fits) {
-      if (p == 0) raise_status(status, kStatusCapacity);
-      continue;
-    }
-    if (p < z.n_oct) {
-      uint4* c4 = reinterpret_cast<uint4*>(O.tags.child);
-      c4[2 * (size_t)g] = make_uint4(0, 0, 0, 0);
-      c4[2 * (size_t)g + 1] = make_uint4(0, 0, 0, 0);
-      O.tags.owner[g] = 0;
-      O.tags.mask[g] = 0;
-    }
-  }
-}
-
+// One CTA per 4,096-node tile of a cloud.
 __global__ void __launch_bounds__(256)
     batch_oct_emit_kernel(BatchDev B, BatchOctDev O, uint32_t* __restrict__ status) {
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < B.N; g += gridDim.x * blockDim.x) {
-    const int c = cloud_of(B.start, B.C, g);
-    const CloudSizes z = cloud_sizes(B, O, c);
-    const int i = g - B.start[c];
-    if (i >= z.n_brt || !z.fits) continue;
-    const OctArgs a = cloud_view(B, O, z);
-    Sizes zz;
-    zz.n_brt = z.n_brt;
-    zz.n_oct = z.n_oct;
-    zz.fits = true;
-    emit_node(kOctMake | kOctLink, i, a, cloud_tags(O, z), zz, status);
+  const int4 d = B.tiles4k[blockIdx.x];
+  const int c = d.z;
+  const CloudSizes z = cloud_sizes(B, O, c);
+  if (!z.fits) {
+    if ((int)blockIdx.x == d.w && threadIdx.x == 0) raise_status(status, kStatusCapacity);
+    return;
   }
+  const int cs = B.start[c];
+  const int end = min(d.y - cs, z.n_brt);
+  const OctArgs a = cloud_view(B, O, z);
+  const OctTags t = cloud_tags(O, z);
+  Sizes zz;
+  zz.n_brt = z.n_brt;
+  zz.n_oct = z.n_oct;
+  zz.fits = true;
+  for (int i = d.x - cs + (int)threadIdx.x; i < end; i += 256)
+    emit_node(kOctMake | kOctLink, i, a, t, zz, status);
 }
 
+// One CTA per 256 OctNode slots of a cloud.
 __global__ void __launch_bounds__(kFinThreads)
-    batch_oct_finalize_kernel(BatchDev B, BatchOctDev O, int total_cap) {
-  __shared__ int s_nodes[kFinThreads * kNodeWords];
-  __shared__ uint8_t s_valid[kFinThreads];
-  int* out_words = reinterpret_cast<int*>(O.nodes);
-  for (int blk = blockIdx.x * kFinThreads; blk < total_cap; blk += gridDim.x * kFinThreads) {
-    const int g = blk + threadIdx.x;
-    bool valid = false;
-    if (g < total_cap) {
-      const int c = cloud_of(B.node_start, B.C, g);
-      const CloudSizes z = cloud_sizes(B, O, c);
-      const int p = g - z.ns;
-      valid = z.fits && z.n_brt >= 1 && p < z.n_oct;
-      if (valid) {
-        const OctArgs a = cloud_view(B, O, z);
-        finalize_slot(true, p, a, cloud_tags(O, z), a.prefix_n[0] / 3,
-                      s_nodes + threadIdx.x * kNodeWords);
-      }
-    }
-    s_valid[threadIdx.x] = valid;
-    __syncthreads();
-    const int count = min(kFinThreads, total_cap - blk);
-    int* dst = out_words + (size_t)blk * kNodeWords;
-    for (int k = threadIdx.x; k < count * kNodeWords; k += kFinThreads)
-      if (s_valid[k / kNodeWords]) dst[k] = s_nodes[k];
-    __syncthreads();
+    batch_oct_finalize_kernel(BatchDev B, BatchOctDev O) {
+  __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
+  const int4 d = B.slot_tiles[blockIdx.x];
+  const CloudSizes z = cloud_sizes(B, O, d.z);
+  const int p0 = d.x - z.ns;
+  const int count = min(d.y - d.x, z.n_oct - p0);
+  if (!z.fits || z.n_brt < 1 || count <= 0) return;
+  const OctArgs a = cloud_view(B, O, z);
+  const int p = p0 + (int)threadIdx.x;
+  if ((int)threadIdx.x < count)
+    finalize_slot(true, p, a, cloud_tags(O, z), a.prefix_n[0] / 3,
+                  s_nodes + threadIdx.x * kNodeWords);
+  __syncthreads();
+  int* dst = reinterpret_cast<int*>(O.nodes + d.x);
+  const int words = count * kNodeWords;
+  int k0 = 0;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+    const int quads = words >> 2;
+    const uint4* src4 = reinterpret_cast<const uint4*>(s_nodes);
+    uint4* dst4 = reinterpret_cast<uint4*>(dst);
+    for (int k = threadIdx.x; k < quads; k += kFinThreads) dst4[k] = src4[k];
+    k0 = quads << 2;
   }
+  for (int k = k0 + threadIdx.x; k < words; k += kFinThreads) dst[k] = s_nodes[k];
 }
 
 __global__ void batch_publish_kernel(BatchDev B, BatchOctDev O, const uint32_t* status,
@@ -471,9 +477,10 @@ struct oct_batch_plan {
   int total_cap = 0;
   octgb::SortPlan sp{};
   std::vector<int> start, node_start, cloud_tile0;
-  std::vector<int4> sort_tiles, tiles4k;
+  std::vector<int4> sort_tiles, tiles4k, slot_tiles;
   // device tables (caller buffer) offsets
-  size_t t_start = 0, t_node_start = 0, t_tile0 = 0, t_sort = 0, t_4k = 0, tables_bytes = 0;
+  size_t t_start = 0, t_node_start = 0, t_tile0 = 0, t_sort = 0, t_4k = 0, t_slots = 0,
+         tables_bytes = 0;
   // workspace offsets
   size_t w_status = 0, w_unique = 0, w_maxslot = 0, w_hist = 0, w_queues = 0, w_lb_u = 0,
          zero_bytes = 0, w_tree = 0, w_base = 0, w_th = 0, w_keys_a = 0, w_keys_b = 0,
@@ -506,6 +513,8 @@ octgb::BatchDev dev_view(const oct_batch_plan* P, const void* tables, const floa
   B.cloud_tile0 = reinterpret_cast<const int*>(t + P->t_tile0);
   B.tiles4k = reinterpret_cast<const int4*>(t + P->t_4k);
   B.T4 = (int)P->tiles4k.size();
+  B.slot_tiles = reinterpret_cast<const int4*>(t + P->t_slots);
+  B.Tn = (int)P->slot_tiles.size();
   return B;
 }
 
@@ -553,6 +562,8 @@ OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_siz
       P->sort_tiles.push_back(make_int4(lo, std::min(lo + tile, P->start[c + 1]), c, P->cloud_tile0[c]));
     for (int lo = P->start[c]; lo < P->start[c + 1]; lo += kBatchTile4k)
       P->tiles4k.push_back(make_int4(lo, std::min(lo + kBatchTile4k, P->start[c + 1]), c, f4));
+    for (int lo = P->node_start[c]; lo < P->node_start[c + 1]; lo += kFinThreads)
+      P->slot_tiles.push_back(make_int4(lo, std::min(lo + kFinThreads, P->node_start[c + 1]), c, 0));
   }
   P->cloud_tile0[n_clouds] = (int)P->sort_tiles.size();
   size_t o = 0;
@@ -566,6 +577,7 @@ OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_siz
   P->t_tile0 = take(4 * (size_t)(n_clouds + 1));
   P->t_sort = take(16 * (P->sort_tiles.size() + 1));
   P->t_4k = take(16 * (P->tiles4k.size() + 1));
+  P->t_slots = take(16 * (P->slot_tiles.size() + 1));
   P->tables_bytes = o;
   const int passes = P->sp.passes, bins = P->sp.bins;
   o = 0;
@@ -616,6 +628,9 @@ OCT_API int oct_batch_upload_tables(const oct_batch_plan* P, void* d_tables, oct
                         cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && !P->tiles4k.empty())
     e = cudaMemcpyAsync(t + P->t_4k, P->tiles4k.data(), 16 * P->tiles4k.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !P->slot_tiles.empty())
+    e = cudaMemcpyAsync(t + P->t_slots, P->slot_tiles.data(), 16 * P->slot_tiles.size(),
                         cudaMemcpyHostToDevice, s);
   // the host vectors live in the plan: wait so the copies have read them
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -685,7 +700,6 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
     const int qgrid = std::max(1, std::min(B.T4, sms * 8));
     batch_unique_kernel<<<qgrid, kBuThreads, 0, s>>>(a, out->codes, B, unique_c, lb_u, queues,
                                                      status);
-    const int ngrid = std::max(1, std::min((P->N + 255) / 256, sms * 16));
     void* tree_ws = w + P->w_tree;
     const TreeScratch TS = tree_scratch_carve_tiles(tree_ws, B.T4);
     e = launch_batch_radix_tree(B.tiles4k, B.T4, B.start, unique_c, out->codes,
@@ -694,8 +708,9 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
                                 out->edge_count, tree_ws, s);
     if (e == cudaSuccess) e = launch_tile_sums_scan(B.T4, TS.tile_sum, TS.tile_prefix, s);
     if (e != cudaSuccess) return batch_fail(e, "batch: tree");
+    const OctTags tags = oct_tags_carve(w + P->w_tags, std::max(P->total_cap, 1));
     batch_prefix_sum_kernel<<<B.T4, 256, 0, s>>>(B, unique_c, out->edge_count, out->prefix_sum,
-                                                 max_slot_c, TS.tile_prefix);
+                                                 max_slot_c, TS.tile_prefix, tags);
     BatchOctDev O;
     O.nodes = out->nodes;
     O.offsets = out->prefix_sum;
@@ -708,11 +723,9 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
     O.left_child = out->tree.left_child;
     O.unique_c = unique_c;
     O.max_slot_c = max_slot_c;
-    O.tags = oct_tags_carve(w + P->w_tags, std::max(P->total_cap, 1));
-    const int cgrid = std::max(1, std::min((P->total_cap + 255) / 256, sms * 16));
-    batch_oct_zero_kernel<<<cgrid, 256, 0, s>>>(B, O, P->total_cap, status);
-    batch_oct_emit_kernel<<<ngrid, 256, 0, s>>>(B, O, status);
-    batch_oct_finalize_kernel<<<cgrid, kFinThreads, 0, s>>>(B, O, P->total_cap);
+    O.tags = tags;
+    batch_oct_emit_kernel<<<B.T4, 256, 0, s>>>(B, O, status);
+    if (B.Tn > 0) batch_oct_finalize_kernel<<<B.Tn, kFinThreads, 0, s>>>(B, O);
     batch_publish_kernel<<<(P->C + 255) / 256, 256, 0, s>>>(B, O, status, d_cloud_counts);
   } else {
     e = cudaMemsetAsync(d_cloud_counts, 0, 16 * (size_t)P->C, s);
