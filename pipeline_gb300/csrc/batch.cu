@@ -92,7 +92,24 @@ __global__ void __launch_bounds__(256)
       cur = d.z;
     }
     const float mn = B.mins[d.z], rg = B.ranges[d.z];
-    for (int i = d.x + threadIdx.x; i < d.y; i += blockDim.x) {
+    // four loads in flight per thread, then the tile's tail
+    constexpr int U = 4;
+    int i = d.x + (int)threadIdx.x;
+    for (; i + (U - 1) * (int)blockDim.x < d.y; i += U * (int)blockDim.x) {
+      float4 p[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) p[u] = ld_stream_f4(pts + i + u * blockDim.x);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        bool ok;
+        const uint32_t c = morton_code(p[u].x, p[u].y, p[u].z, mn, rg, ok);
+        bad |= !ok;
+        keys[i + u * blockDim.x] = c;
+        for (int ps = 0; ps < passes; ++ps)
+          atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);
+      }
+    }
+    for (; i < d.y; i += blockDim.x) {
       const float4 p = ld_stream_f4(pts + i);
       bool ok;
       const uint32_t c = morton_code(p.x, p.y, p.z, mn, rg, ok);
@@ -141,18 +158,20 @@ __global__ void __launch_bounds__(1024)
 }
 
 // In place: th[t][d] = where tile t's keys of digit d start, for the tiles of
-// cloud blockIdx.x (blocks: clouds x 32-digit groups; 32 digits x 32 tile
-// groups per block).
-__global__ void __launch_bounds__(1024)
+// cloud blockIdx.x (blocks: clouds x 32-digit groups; 32 digits x
+// kTsGroups tile groups per block).
+constexpr int kTsGroups = 8;
+__global__ void __launch_bounds__(32 * kTsGroups)
     batch_tile_scan_kernel(uint32_t* __restrict__ th, int bins, const uint32_t* __restrict__ base,
                            int passes, int pass, BatchDev B) {
-  __shared__ uint32_t part[32][33];
+  __shared__ uint32_t part[kTsGroups][33];
   const int c = blockIdx.x;
   const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int d = blockIdx.y * 32 + l;
   const int ta = B.cloud_tile0[c], tb = B.cloud_tile0[c + 1];
   const int nt = tb - ta;
-  const int t0 = ta + (int)((long long)nt * g / 32), t1 = ta + (int)((long long)nt * (g + 1) / 32);
+  const int t0 = ta + (int)((long long)nt * g / kTsGroups);
+  const int t1 = ta + (int)((long long)nt * (g + 1) / kTsGroups);
   uint32_t sum = 0;
   if (d < bins)
     for (int t = t0; t < t1; ++t) sum += th[(size_t)t * bins + d];
@@ -688,8 +707,8 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
       const int shift = p * rb;
       e = launch_tile_hist(rb, a, P->N, shift, B.sort_tiles, B.Ts, th, s);
       if (e != cudaSuccess) break;
-      batch_tile_scan_kernel<<<dim3(P->C, (bins + 31) / 32), 1024, 0, s>>>(th, bins, base, passes,
-                                                                           p, B);
+      batch_tile_scan_kernel<<<dim3(P->C, (bins + 31) / 32), 32 * kTsGroups, 0, s>>>(
+          th, bins, base, passes, p, B);
       e = launch_pass(sp, p > 0, a, b, shift, nullptr, nullptr, nullptr, th, status, nullptr, s,
                       B.sort_tiles, B.Ts);
       uint32_t* t = a;
