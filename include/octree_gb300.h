@@ -82,7 +82,8 @@ typedef enum oct_status {
   OCT_ERR_CUDA = 3,        /* a CUDA runtime call or launch failed */
   OCT_ERR_DEVICE = 4,      /* the device status word is non-zero (sync calls) */
   OCT_ERR_CAPACITY = 5,    /* octree node buffer too small (sync calls) */
-  OCT_ERR_TOO_LARGE = 6    /* size above a fixed limit (oct_sort_keys_noalloc) */
+  OCT_ERR_TOO_LARGE = 6    /* size above a fixed limit (oct_sort_keys_noalloc,
+                              OCT_MAX_OCTREE_NODES) */
 } oct_status;
 
 /* Device status word bits. */
@@ -93,6 +94,11 @@ typedef enum oct_status {
 
 /* Largest point / key count accepted (counts travel in 30-bit fields). */
 #define OCT_MAX_N ((1 << 30) - 1)
+
+/* Largest radix-node count the octree stages (7-8) accept: their write tags
+ * carry the radix node's index in 27 bits. Whole builds with an octree take
+ * up to OCT_MAX_OCTREE_NODES + 1 points per cloud. */
+#define OCT_MAX_OCTREE_NODES ((1 << 27) - 1)
 
 /* Library version and the device architecture it was built for (e.g. 1033 = sm_103a). */
 OCT_API int oct_version(void);

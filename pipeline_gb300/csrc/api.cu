@@ -283,6 +283,7 @@ static int octree_stage(int mode, oct_node* nodes, int n_oct_nodes, const int32_
                         oct_stream_t stream) {
   if (n_nodes < 0 || n_oct_nodes < 0 || n_nodes > OCT_MAX_N || n_oct_nodes > OCT_MAX_N)
     return OCT_ERR_INVALID_ARG;
+  if (n_nodes > OCT_MAX_OCTREE_NODES) return OCT_ERR_TOO_LARGE;
   if (n_nodes == 0 || n_oct_nodes == 0) return OCT_OK;
   if (!nodes || !offsets || !counts || !codes || !prefix_n || !parents || !workspace ||
       !aligned(workspace, 256))
@@ -340,6 +341,7 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
                       const oct_build_outputs* out, void* workspace, size_t workspace_bytes,
                       oct_stream_t stream, Recorder* rec) {
   if (n < 0 || n > OCT_MAX_N || !out || !out->d_counts) return OCT_ERR_INVALID_ARG;
+  if (out->nodes_capacity > 0 && n > OCT_MAX_OCTREE_NODES + 1) return OCT_ERR_TOO_LARGE;
   cudaStream_t s = S(stream);
   if (n == 0) {
     OCT_TRY(cudaMemsetAsync(out->d_counts, 0, 4 * sizeof(int32_t), s), "oct_build_octree");

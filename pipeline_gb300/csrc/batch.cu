@@ -552,7 +552,8 @@ OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_siz
   P->start.resize(n_clouds + 1);
   P->node_start.resize(n_clouds + 1);
   for (int c = 0; c < n_clouds; ++c) {
-    if (h_sizes[c] < 0 || (h_node_caps && h_node_caps[c] < 0)) {
+    if (h_sizes[c] < 0 || h_sizes[c] > OCT_MAX_OCTREE_NODES + 1 ||
+        (h_node_caps && h_node_caps[c] < 0)) {
       delete P;
       return nullptr;
     }

@@ -788,6 +788,7 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
   using namespace octgb;
   if (!lsort_args_ok(n, n_buckets, max_segments) || !model || !out || !out->d_counts)
     return OCT_ERR_INVALID_ARG;
+  if (out->nodes_capacity > 0 && n > OCT_MAX_OCTREE_NODES + 1) return OCT_ERR_TOO_LARGE;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (n == 0) {
     const cudaError_t e = cudaMemsetAsync(out->d_counts, 0, 4 * sizeof(int32_t), s);

@@ -69,6 +69,22 @@ def test_invalid_arguments_rejected_before_any_device_work():
     assert lib.oct_unique(al, 100, al, al, 8, None, None) == _lib.OCT_ERR_WORKSPACE
 
 
+def test_octree_node_limit_rejected_before_any_device_work():
+    """Octree write tags hold the radix-node index in 27 bits: larger octree
+    stages and whole builds with an octree answer OCT_ERR_TOO_LARGE."""
+    lib = _lib.load()
+    big = (1 << 27) - 1 + 1
+    assert lib.oct_make_oct_nodes(None, 10, None, None, None, None, None, 0.0, 1.0, big, None, 0,
+                                  None, None) == _lib.OCT_ERR_TOO_LARGE
+    out = _lib.OctBuildOutputs()
+    out.nodes_capacity = 1
+    out.d_counts = C.c_void_p(0x100000)
+    assert lib.oct_build_octree(None, big + 1, 0.0, 1.0, C.byref(out), None, 0, None) == \
+        _lib.OCT_ERR_TOO_LARGE
+    sizes = (C.c_int32 * 2)(1000, big + 1)
+    assert not lib.oct_batch_plan_create(2, sizes, None)
+
+
 def test_host_generator_matches_reference(golden):
     """oct_init_random_vec4 reproduces k_InitRandomVec4's points."""
     from pipeline_gb300.kernels import k_InitRandomVec4
