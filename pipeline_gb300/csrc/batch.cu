@@ -427,7 +427,7 @@ __device__ __forceinline__ OctTags cloud_tags(const BatchOctDev& O, const CloudS
 }
 
 // One CTA per 4,096-node tile of a cloud.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 6)
     batch_oct_emit_kernel(BatchDev B, BatchOctDev O, uint32_t* __restrict__ status) {
   const int4 d = B.tiles4k[blockIdx.x];
   const int c = d.z;
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // One CTA per 256 OctNode slots of a cloud.
-__global__ void __launch_bounds__(kFinThreads)
+__global__ void __launch_bounds__(kFinThreads, 5)
     batch_oct_finalize_kernel(BatchDev B, BatchOctDev O) {
   __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
   const int4 d = B.slot_tiles[blockIdx.x];

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
   }
 }
 
-__global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctTags t,
+__global__ void __launch_bounds__(256, 8) oct_emit_kernel(int mode, OctArgs a, OctTags t,
                                                        uint32_t* __restrict__ status,
                                                        bool report_capacity) {
   const Sizes z = read_sizes(a);
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) oct_emit_kernel(int mode, OctArgs a, OctT
     emit_node(mode, i, a, t, z, status);
 }
 
-__global__ void __launch_bounds__(kFinThreads) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
+__global__ void __launch_bounds__(kFinThreads, 6) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
   __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
   const Sizes z = read_sizes(a);
   if (!z.fits || z.n_brt < 1) return;
