@@ -113,9 +113,7 @@ cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* c
 // sorted unique Morton codes), from the adjacent deltas; with ec != nullptr
 // also the edge counts. scratch: tree_scratch_bytes(n_host), 256-aligned.
 struct TreeScratch {
-  uint8_t* D;          // [tiles * 4096] adjacent deltas
-  int* tile_last;      // [tiles * 32] last position of the tile with D < v, or -1
-  int* tile_first;     // [tiles * 32] first position of the tile with D < v, or INT_MAX
+  uint8_t* D;          // [tiles * 4096] adjacent deltas, tile-major
   uint8_t* tile_min;   // [tiles rounded up to 512] smallest D of the tile
   int* tile_sum;       // [tiles] sum of the edge counts of the tile's 4,096 nodes
   uint32_t* tile_prefix;  // [tiles] exclusive prefix of tile_sum

@@ -22,13 +22,13 @@
 // (kernels/05_edge_count.cpp:3-16) is computed here as well.
 //
 // Two kernels over tiles of 4,096 positions:
-//   tree_tiles_kernel  D as bytes; per tile, for every value v the first and
-//                      last position with D < v, and the tile's smallest D;
+//   tree_tiles_kernel  D as bytes and each tile's smallest D;
 //   tree_nodes_kernel  nearest smaller deltas inside each 32-position chunk
 //                      from five ballots over the bits of D, across the
 //                      tile's chunks from prefix / suffix tables in shared
-//                      memory, across tiles from the tile tables (rare: only
-//                      the tile's running minima); then every output of the
+//                      memory, across tiles (rare: only the tile's running
+//                      minima) by a warp-wide scan of the tile minima and then
+//                      of the found tile's deltas; then every output of the
 //                      node split at each position.
 #include <climits>
 
@@ -52,8 +52,8 @@ static int tt_tiles(int n) { return ((n > 1 ? n : 1) + kTtTile - 1) / kTtTile; }
 
 size_t tree_scratch_bytes_tiles(int tiles) {
   const size_t t = (size_t)(tiles > 1 ? tiles : 1);
-  return align_up(t * kTtTile, 256) + 2 * align_up(t * 32 * sizeof(int), 256) +
-         align_up(align_up(t, kTtMinBlock), 256) + 2 * align_up(t * sizeof(int), 256);
+  return align_up(t * kTtTile, 256) + align_up(align_up(t, kTtMinBlock), 256) +
+         2 * align_up(t * sizeof(int), 256);
 }
 
 TreeScratch tree_scratch_carve_tiles(void* base, int tiles) {
@@ -63,10 +63,6 @@ TreeScratch tree_scratch_carve_tiles(void* base, int tiles) {
   S.tiles = (int)t;
   S.D = reinterpret_cast<uint8_t*>(p);
   p += align_up(t * kTtTile, 256);
-  S.tile_last = reinterpret_cast<int*>(p);
-  p += align_up(t * 32 * sizeof(int), 256);
-  S.tile_first = reinterpret_cast<int*>(p);
-  p += align_up(t * 32 * sizeof(int), 256);
   S.tile_min = reinterpret_cast<uint8_t*>(p);
   p += align_up(align_up(t, kTtMinBlock), 256);
   S.tile_sum = reinterpret_cast<int*>(p);
@@ -160,7 +156,6 @@ template <class Map>
 __global__ void __launch_bounds__(kTtAThreads)
     tree_tiles_kernel(Map map, const uint32_t* __restrict__ codes_all, TreeScratch S) {
   constexpr int kWarps = kTtAThreads / 32;
-  __shared__ int s_last[kWarps][32], s_first[kWarps][32];
   __shared__ uint32_t s_min[kWarps];
   const TileInfo I = map(blockIdx.x);
   const int n = I.n, t = I.t, t0 = I.lo;
@@ -172,70 +167,69 @@ __global__ void __launch_bounds__(kTtAThreads)
     for (int k = S.tiles + (int)threadIdx.x; k < pad; k += kTtAThreads)
       S.tile_min[k] = (uint8_t)kTtAbsent;
   }
-  int last = -1, first = INT_MAX;  // lane v: positions with D < v
   uint32_t dmin = kTtAbsent;
   if (t0 < n) {
-    uint32_t lm[5];
-    bit_masks((uint32_t)lane, lm);
-    constexpr int kStep = 4;  // chunks whose codes are loaded together
-    for (int c0 = warp; c0 < kTtChunks; c0 += kWarps * kStep) {
-      uint32_t cp[kStep], cx[kStep];
+    // a thread takes 4 consecutive positions per step: 16-byte code loads,
+    // 4-byte delta stores; the code after the fourth comes from the next lane
+    const uint4* c4 = reinterpret_cast<const uint4*>(codes);
+    const bool vec = (reinterpret_cast<uintptr_t>(codes) & 15) == 0;
+    for (int base = t0 + 4 * (int)threadIdx.x; base < t0 + kTtTile; base += 4 * kTtAThreads) {
+      uint32_t c[5];
+      if (vec && base + 4 <= n + 1) {
+        const uint4 v = c4[base >> 2];
+        c[0] = v.x;
+        c[1] = v.y;
+        c[2] = v.z;
+        c[3] = v.w;
+      } else {
 #pragma unroll
-      for (int j = 0; j < kStep; ++j) {
-        const int p = t0 + 32 * (c0 + j * kWarps) + lane;
-        cp[j] = p <= n ? codes[p] : 0u;  // codes[0..n]
-        cx[j] = (lane == 31 && p + 1 <= n) ? codes[p + 1] : 0u;
+        for (int k = 0; k < 4; ++k) c[k] = base + k <= n ? codes[base + k] : 0u;
       }
+      c[4] = __shfl_down_sync(kFull, c[0], 1);
+      if (lane == 31) c[4] = base + 4 <= n ? codes[base + 4] : 0u;
+      uint32_t packed = 0;
 #pragma unroll
-      for (int j = 0; j < kStep; ++j) {
-        const int c = c0 + j * kWarps;
-        const int p = t0 + 32 * c + lane;
-        uint32_t cn = __shfl_down_sync(kFull, cp[j], 1);
-        if (lane == 31) cn = cx[j];
-        const uint32_t d = p < n ? tt_delta(cp[j], cn) : kTtAbsent;
-        Dt[32 * c + lane] = (uint8_t)d;
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t d = base + k < n ? tt_delta(c[k], c[k + 1]) : kTtAbsent;
         dmin = min(dmin, d);
-        uint32_t b[5];
-        value_ballots(d, b);
-        const uint32_t lt = lanes_below(b, lm);
-        if (lt) {
-          last = t0 + 32 * c + 31 - __clz(lt);
-          if (first == INT_MAX) first = t0 + 32 * c + __ffs(lt) - 1;
-        }
+        packed |= d << (8 * k);
       }
+      *reinterpret_cast<uint32_t*>(Dt + (base - t0)) = packed;
     }
+  } else {
+    for (int k = threadIdx.x; k < kTtTile / 4; k += kTtAThreads)
+      reinterpret_cast<uint32_t*>(Dt)[k] = kTtAbsent * 0x01010101u;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dmin = min(dmin, __shfl_xor_sync(kFull, dmin, o));
-  s_last[warp][lane] = last;
-  s_first[warp][lane] = first;
   if (lane == 0) s_min[warp] = dmin;
   __syncthreads();
-  if (warp == 0) {
-    int l = -1, f = INT_MAX;
+  if (threadIdx.x == 0) {
     uint32_t m = kTtAbsent;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      l = max(l, s_last[w][lane]);
-      f = min(f, s_first[w][lane]);
-      m = min(m, s_min[w]);
-    }
-    S.tile_last[t * 32 + lane] = l;
-    S.tile_first[t * 32 + lane] = f;
-    if (lane == 0) {
-      S.tile_min[t] = (uint8_t)m;
-      S.tile_sum[t] = 0;
-    }
+    for (int w = 0; w < kWarps; ++w) m = min(m, s_min[w]);
+    S.tile_min[t] = (uint8_t)m;
+    S.tile_sum[t] = 0;
   }
+}
+
+// Bytes here are at most 31 and so is x: (byte | 0x80) - x keeps the high
+// bit exactly when byte >= x, with no borrow between bytes.
+__device__ __forceinline__ uint32_t high_bits_below(uint32_t w, uint32_t x4) {
+  return ~((w | 0x80808080u) - x4) & 0x80808080u;
 }
 
 // Bit j set when byte j of w (16 bytes) is below x.
 __device__ __forceinline__ uint32_t bytes_below(const uint4& w, uint32_t x) {
+  const uint32_t x4 = x * 0x01010101u;
   const uint32_t v[4] = {w.x, w.y, w.z, w.w};
   uint32_t m = 0;
 #pragma unroll
-  for (int j = 0; j < 16; ++j)
-    if (((v[j >> 2] >> (8 * (j & 3))) & 0xffu) < x) m |= 1u << j;
+  for (int k = 0; k < 4; ++k) {
+    // gather the four high bits (7, 15, 23, 31) into bits 21..24
+    const uint32_t h = ((high_bits_below(v[k], x4) >> 7) * 0x00204081u) >> 21;
+    m |= (h & 0xFu) << (4 * k);
+  }
   return m;
 }
 
@@ -279,6 +273,39 @@ __device__ int tiles_scan_right(const uint8_t* __restrict__ tmin, int lo, int hi
     }
   }
   return -1;
+}
+
+// Last (first) position of tile tt's deltas below x; the tile holds one.
+__device__ int tile_last_below(const TreeScratch& S, const TileInfo& I, int tt, uint32_t x,
+                               int lane) {
+  const uint8_t* Dt = S.D + (size_t)tt * kTtTile;
+  for (int blk = kTtTile / 512 - 1; blk >= 0; --blk) {
+    const uint4 w = reinterpret_cast<const uint4*>(Dt + blk * 512)[lane];
+    const uint32_t m = bytes_below(w, x);
+    const uint32_t any = __ballot_sync(kFull, m != 0);
+    if (any) {
+      const int L = 31 - __clz(any);
+      const uint32_t mL = __shfl_sync(kFull, m, L);
+      return (tt - I.t_first) * kTtTile + blk * 512 + L * 16 + 31 - __clz(mL);
+    }
+  }
+  return -1;
+}
+
+__device__ int tile_first_below(const TreeScratch& S, const TileInfo& I, int tt, uint32_t x,
+                                int lane) {
+  const uint8_t* Dt = S.D + (size_t)tt * kTtTile;
+  for (int blk = 0; blk < kTtTile / 512; ++blk) {
+    const uint4 w = reinterpret_cast<const uint4*>(Dt + blk * 512)[lane];
+    const uint32_t m = bytes_below(w, x);
+    const uint32_t any = __ballot_sync(kFull, m != 0);
+    if (any) {
+      const int L = __ffs(any) - 1;
+      const uint32_t mL = __shfl_sync(kFull, m, L);
+      return (tt - I.t_first) * kTtTile + blk * 512 + L * 16 + __ffs(mL) - 1;
+    }
+  }
+  return I.n;
 }
 
 struct TreeOut {
@@ -399,23 +426,34 @@ __global__ void __launch_bounds__(kTtBThreads)
       else if (s_pl[c][xv] >= 0) a = t0 + s_pl[c][xv];
       if (nv != 0xFF) b = t0 + 32 * c + (int)nv;
       else if (s_sf[c][xv] < kTtTile) b = t0 + s_sf[c][xv];
-      if (a == -2) {  // the previous tile first
-        if (t == I.t_first) a = -1;
-        else if (S.tile_last[(t - 1) * 32 + xv] >= 0) a = S.tile_last[(t - 1) * 32 + xv];
+      if (a == -2) {  // the end of the previous tile first
+        if (t == I.t_first) {
+          a = -1;
+        } else {
+          const uint4 w = *reinterpret_cast<const uint4*>(S.D + (size_t)t * kTtTile - 16);
+          const uint32_t m = bytes_below(w, xv);
+          if (m) a = t0 - 16 + 31 - __clz(m);
+        }
       }
-      if (b == -2) {
-        if (t + 1 > I.t_last) b = n;
-        else if (S.tile_first[(t + 1) * 32 + xv] != INT_MAX) b = S.tile_first[(t + 1) * 32 + xv];
+      if (b == -2) {  // the start of the next tile first
+        if (t == I.t_last) {
+          b = n;
+        } else {
+          const uint4 w = *reinterpret_cast<const uint4*>(S.D + (size_t)(t + 1) * kTtTile);
+          const uint32_t m = bytes_below(w, xv);
+          if (m) b = t0 + kTtTile + __ffs(m) - 1;
+        }
       }
     }
-    // Farther tiles: one warp-wide scan of the tile minima per query.
+    // Other tiles: one warp-wide scan of the tile minima per query, then of
+    // the found tile's deltas.
     uint32_t need = __ballot_sync(kFull, live && a == -2);
     while (need) {
       const int src = __ffs(need) - 1;
       need &= need - 1;
       const uint32_t qx = __shfl_sync(kFull, xv, src);
-      const int tt = tiles_scan_left(S.tile_min, I.t_first, t - 2, qx, lane);
-      const int ans = tt >= 0 ? S.tile_last[tt * 32 + qx] : -1;
+      const int tt = tiles_scan_left(S.tile_min, I.t_first, t - 1, qx, lane);
+      const int ans = tt >= 0 ? tile_last_below(S, I, tt, qx, lane) : -1;
       if (lane == src) a = ans;
     }
     need = __ballot_sync(kFull, live && b == -2);
@@ -423,8 +461,8 @@ __global__ void __launch_bounds__(kTtBThreads)
       const int src = __ffs(need) - 1;
       need &= need - 1;
       const uint32_t qx = __shfl_sync(kFull, xv, src);
-      const int tt = tiles_scan_right(S.tile_min, t + 2, I.t_last, qx, lane);
-      const int ans = tt >= 0 ? S.tile_first[tt * 32 + qx] : n;
+      const int tt = tiles_scan_right(S.tile_min, t + 1, I.t_last, qx, lane);
+      const int ans = tt >= 0 ? tile_first_below(S, I, tt, qx, lane) : n;
       if (lane == src) b = ans;
     }
     if (!live) continue;
