@@ -51,7 +51,7 @@ struct SortPlan {
   int tile;
   int tiles;
   SortConfig cfg;
-  size_t hist_off, counter_off, lookback_off, base_off, tile_hist_off;
+  size_t hist_off, counter_off, lookback_off, tile_part_off, base_off, tile_hist_off;
   size_t zero_bytes;  // [0, zero_bytes) is cleared before each sort
   size_t bytes;       // whole control block
 };

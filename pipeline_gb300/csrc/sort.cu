@@ -387,11 +387,20 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
 }
 
 // Per-tile digit counts for SCAN 1 passes: th[tile * BINS + b].
+// Reduce-then-scan over tiles: the tiles are cut into kScanSplits contiguous
+// splits; tile_hist also adds each tile's counts into its split's partial
+// sums, so the tile scan runs every split in its own CTAs.
+constexpr int kScanSplits = 16;
+
+__host__ __device__ __forceinline__ int split_tiles(int tiles) {
+  return (tiles + kScanSplits - 1) / kScanSplits;
+}
+
 template <int RB>
 __global__ void __launch_bounds__(256)
     tile_hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tile_keys,
                      uint32_t* __restrict__ th, const uint32_t* __restrict__ gate,
-                     const int4* __restrict__ tdesc) {
+                     const int4* __restrict__ tdesc, uint32_t* __restrict__ part, int tiles) {
   if (gate && *gate == 0) return;
   constexpr int BINS = 1 << RB;
   __shared__ uint32_t h[BINS];
@@ -414,34 +423,39 @@ __global__ void __launch_bounds__(256)
     atomicAdd(&h[(keys[i] >> shift) & (BINS - 1)], 1u);
   __syncthreads();
   for (int b = threadIdx.x; b < BINS; b += 256) th[(size_t)t * BINS + b] = h[b];
+  if (part) {
+    uint32_t* ps = part + (size_t)(t / split_tiles(tiles)) * BINS;
+    for (int b = threadIdx.x; b < BINS; b += 256)
+      if (h[b]) atomicAdd(ps + b, h[b]);
+  }
 }
 
 // In place: th[t][b] becomes the output index where tile t's keys of digit b
 // start (bin_base[b] + counts of earlier tiles). Block: 32 digits x 32 tile
-// groups; lanes run along digits, so every load is a coalesced 128 B row part.
+// groups of one split (blockIdx.y); lanes run along digits, so every load is a
+// coalesced 128 B row part. A split starts from the partial sums of the
+// splits before it.
 __global__ void __launch_bounds__(1024)
-    tile_scan_kernel(uint32_t* __restrict__ th, int tiles, int bins,
-                     const uint32_t* __restrict__ bin_base, const uint32_t* __restrict__ gate) {
+    tile_scan_split_kernel(uint32_t* __restrict__ th, int tiles, int bins,
+                           const uint32_t* __restrict__ bin_base, const uint32_t* __restrict__ part,
+                           const uint32_t* __restrict__ gate) {
   if (gate && *gate == 0) return;
-  __shared__ uint32_t part[32][33];
+  __shared__ uint32_t sums[32][33];
   const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + l;
-  const int t0 = (int)((long long)tiles * g / 32), t1 = (int)((long long)tiles * (g + 1) / 32);
+  const int per = split_tiles(tiles);
+  const int ta = blockIdx.y * per, tb = min(tiles, ta + per);
+  const int nt = max(tb - ta, 0);
+  const int t0 = ta + nt * g / 32, t1 = ta + nt * (g + 1) / 32;
   uint32_t sum = 0;
-  if (d < bins) {
-    int t = t0;
-    for (; t + 4 <= t1; t += 4) {
-      const uint32_t a = th[(size_t)t * bins + d], b = th[(size_t)(t + 1) * bins + d];
-      const uint32_t c = th[(size_t)(t + 2) * bins + d], e = th[(size_t)(t + 3) * bins + d];
-      sum += a + b + c + e;
-    }
-    for (; t < t1; ++t) sum += th[(size_t)t * bins + d];
-  }
-  part[g][l] = sum;
+  if (d < bins)
+    for (int t = t0; t < t1; ++t) sum += th[(size_t)t * bins + d];
+  sums[g][l] = sum;
   __syncthreads();
   if (d >= bins) return;
   uint32_t run = bin_base[d];
-  for (int k = 0; k < g; ++k) run += part[k][l];
+  for (int s = 0; s < (int)blockIdx.y; ++s) run += part[(size_t)s * bins + d];
+  for (int k = 0; k < g; ++k) run += sums[k][l];
   for (int t = t0; t < t1; ++t) {
     const uint32_t v = th[(size_t)t * bins + d];
     th[(size_t)t * bins + d] = run;
@@ -483,7 +497,10 @@ SortPlan sort_plan_cfg(int n, int key_bits, SortConfig cfg) {
   p.counter_off = align_up(p.hist_off + sizeof(uint32_t) * p.passes * p.bins, 256);
   p.lookback_off = align_up(p.counter_off + sizeof(uint32_t) * 64, 256);
   const size_t lb_bytes = p.cfg.scan == 0 ? sizeof(uint32_t) * (size_t)p.passes * p.tiles * p.bins : 0;
-  p.zero_bytes = align_up(p.lookback_off + lb_bytes, 256);
+  p.tile_part_off = align_up(p.lookback_off + lb_bytes, 256);
+  const size_t part_bytes =
+      p.cfg.scan == 1 ? sizeof(uint32_t) * (size_t)p.passes * kScanSplits * p.bins : 0;
+  p.zero_bytes = align_up(p.tile_part_off + part_bytes, 256);
   p.base_off = p.zero_bytes;
   p.tile_hist_off = align_up(p.base_off + sizeof(uint32_t) * p.passes * p.bins, 256);
   const size_t th_bytes = p.cfg.scan == 1 ? sizeof(uint32_t) * (size_t)p.tiles * p.bins : 0;
@@ -613,6 +630,7 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
   uint32_t* counters = reinterpret_cast<uint32_t*>(c + plan->counter_off);
   uint32_t* lookback = reinterpret_cast<uint32_t*>(c + plan->lookback_off);
   uint32_t* th = reinterpret_cast<uint32_t*>(c + plan->tile_hist_off);
+  uint32_t* part = reinterpret_cast<uint32_t*>(c + plan->tile_part_off);
   if (plan->radix_bits == 10)
     hist_scan_kernel<10><<<plan->passes, 1024, 0, s>>>(hist, base, gate);
   else
@@ -625,14 +643,15 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
   for (int p = 0; p < plan->passes; ++p) {
     const int shift = p * plan->radix_bits;
     if (plan->cfg.scan == 1) {
+      uint32_t* pp = part + (size_t)p * kScanSplits * plan->bins;
       if (plan->radix_bits == 10)
         tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gate,
-                                                         nullptr);
+                                                         nullptr, pp, plan->tiles);
       else
         tile_hist_kernel<8><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gate,
-                                                        nullptr);
-      tile_scan_kernel<<<(plan->bins + 31) / 32, 1024, 0, s>>>(th, plan->tiles, plan->bins,
-                                                               base + p * plan->bins, gate);
+                                                        nullptr, pp, plan->tiles);
+      tile_scan_split_kernel<<<dim3((plan->bins + 31) / 32, kScanSplits), 1024, 0, s>>>(
+          th, plan->tiles, plan->bins, base + p * plan->bins, pp, gate);
     }
     uint32_t* lb = lookback + (size_t)p * plan->tiles * plan->bins;
     e = launch_pass(*plan, p > 0, a, b, shift, base + p * plan->bins,
@@ -662,9 +681,11 @@ cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPl
 cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
                              const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s) {
   if (radix_bits == 10)
-    tile_hist_kernel<10><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc);
+    tile_hist_kernel<10><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc, nullptr,
+                                               tiles);
   else
-    tile_hist_kernel<8><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc);
+    tile_hist_kernel<8><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc, nullptr,
+                                              tiles);
   return cudaGetLastError();
 }
 
