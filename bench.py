@@ -439,13 +439,14 @@ def host_link_bound(dev, pinned_in, pinned_out, in_bytes: int, out_bytes: int) -
 def build_launches() -> int:
     """Kernel launches of one plain build under the active sort shape:
     Morton, digit-base scan, per pass (tile histogram + tile scan +) pass,
-    unique, tree tiles + tree nodes, tile-sum scan + prefix sum (which
-    clears the octree tags), octree emit/finalize, counts."""
+    unique (run-head count, their scan, compaction with the deltas), tree
+    nodes, tile-sum scan + prefix sum (which clears the octree tags), octree
+    emit/finalize, counts."""
     from pipeline_gb300 import autotune
 
     rb, _, _, scan = autotune.get_config()
     passes = (30 + rb - 1) // rb
-    return 2 + passes * (3 if scan == 1 else 1) + 1 + 2 + 2 + 2 + 1
+    return 2 + passes * (3 if scan == 1 else 1) + 3 + 1 + 2 + 2 + 1
 
 
 def profile_only(args):
@@ -749,8 +750,9 @@ def sort_bar_workload(dev, flush, reps, pts):
 
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_uniform_4m.txt")
 TRAFFIC_POINTS = 4194304
-TRAFFIC_KERNELS = {"morton+histogram": ["morton_kernel<10, 1>"], "unique": ["unique_kernel"],
-                   "radix tree+edge count": ["tree_tiles_kernel", "tree_nodes_kernel"],
+TRAFFIC_KERNELS = {"morton+histogram": ["morton_kernel<10, 1>"],
+                   "unique": ["unique_count_kernel", "unique_deltas_kernel"],
+                   "radix tree+edge count": ["tree_nodes_kernel"],
                    "prefix sum": ["tile_sums_scan_kernel", "edge_scan_kernel"],
                    "octree emit": ["oct_emit_kernel"],
                    "octree finalize": ["oct_finalize_kernel"]}

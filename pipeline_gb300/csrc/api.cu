@@ -370,15 +370,15 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
   uint32_t* sorted = keys_a;
   OCT_TRY(launch_sort_passes(keys_a, keys_b, &L.sort, w + L.sort_off, m.status, s, &sorted, rec),
           "build: sort");
-  OCT_TRY(launch_unique(sorted, out->codes, n, m.unique, &L.uniq, w + L.uniq_off, m.status, s),
+  // Unique with the deltas of adjacent unique codes on the side; the tree
+  // (with the edge counts) comes from those deltas.
+  OCT_TRY(launch_unique_deltas(sorted, n, out->codes, m.unique, w + L.tree_off, s),
           "build: unique");
   mark(rec, s);
-  // The codes are the build's own sorted unique Morton codes: the tree comes
-  // from their adjacent deltas, with the edge counts.
-  OCT_TRY(launch_radix_tree_sorted(n, m.unique, out->codes, out->tree.prefix_n,
-                                   out->tree.has_leaf_left, out->tree.has_leaf_right,
-                                   out->tree.left_child, out->tree.parent, out->edge_count,
-                                   w + L.tree_off, s),
+  OCT_TRY(launch_radix_tree_from_deltas(n, m.unique, out->codes, out->tree.prefix_n,
+                                        out->tree.has_leaf_left, out->tree.has_leaf_right,
+                                        out->tree.left_child, out->tree.parent, out->edge_count,
+                                        w + L.tree_off, s),
           "build: radix tree");
   mark(rec, s);
   const OctTags tags = oct_tags_carve(w + L.tags_off, out->nodes_capacity);

@@ -117,10 +117,27 @@ struct TreeScratch {
   uint8_t* tile_min;   // [tiles rounded up to 512] smallest D of the tile
   int* tile_sum;       // [tiles] sum of the edge counts of the tile's 4,096 nodes
   uint32_t* tile_prefix;  // [tiles] exclusive prefix of tile_sum
+  int* tile_heads;     // [tiles] run heads of a 4,096-key tile of the sorted keys
+  uint32_t* tile_upos; // [tiles] exclusive prefix of tile_heads
   int tiles;
 };
 size_t tree_scratch_bytes(int n_host);
 TreeScratch tree_scratch_carve(void* base, int n_host);
+// Stage 3 fused with the deltas for the whole-cloud build: the run heads of the
+// sorted keys are counted per 4,096-key tile and scanned (no look-back); the
+// compaction writes the unique codes, U to *d_unique and, for each unique code
+// but the first, the delta to the one before it into the tree scratch (and the
+// tiles' smallest deltas), so only tree_nodes_kernel remains of stage 4.
+cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_out, int* d_unique,
+                                 void* tree_scratch, cudaStream_t s);
+// The radix tree (and edge counts) from deltas already in the scratch.
+cudaError_t launch_radix_tree_from_deltas(int n_host, const int* d_unique, const uint32_t* codes,
+                                          uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
+                                          int* left_child, int* parent, int* ec, void* scratch,
+                                          cudaStream_t s);
+// Exclusive scan of `tiles` counts into prefix (one CTA); total to *total_out.
+cudaError_t launch_tile_counts_scan(int tiles, const int* counts, uint32_t* prefix,
+                                    int* total_out, cudaStream_t s);
 size_t tree_scratch_bytes_tiles(int tiles);
 TreeScratch tree_scratch_carve_tiles(void* base, int tiles);
 // Batched clouds: tiles {first, end, cloud, first tile of cloud} of 4,096

@@ -53,7 +53,7 @@ static int tt_tiles(int n) { return ((n > 1 ? n : 1) + kTtTile - 1) / kTtTile; }
 size_t tree_scratch_bytes_tiles(int tiles) {
   const size_t t = (size_t)(tiles > 1 ? tiles : 1);
   return align_up(t * kTtTile, 256) + align_up(align_up(t, kTtMinBlock), 256) +
-         2 * align_up(t * sizeof(int), 256);
+         4 * align_up(t * sizeof(int), 256);
 }
 
 TreeScratch tree_scratch_carve_tiles(void* base, int tiles) {
@@ -68,6 +68,10 @@ TreeScratch tree_scratch_carve_tiles(void* base, int tiles) {
   S.tile_sum = reinterpret_cast<int*>(p);
   p += align_up(t * sizeof(int), 256);
   S.tile_prefix = reinterpret_cast<uint32_t*>(p);
+  p += align_up(t * sizeof(int), 256);
+  S.tile_heads = reinterpret_cast<int*>(p);
+  p += align_up(t * sizeof(int), 256);
+  S.tile_upos = reinterpret_cast<uint32_t*>(p);
   return S;
 }
 
@@ -302,7 +306,8 @@ __device__ int tile_first_below(const TreeScratch& S, const TileInfo& I, int tt,
     if (any) {
       const int L = __ffs(any) - 1;
       const uint32_t mL = __shfl_sync(kFull, m, L);
-      return (tt - I.t_first) * kTtTile + blk * 512 + L * 16 + __ffs(mL) - 1;
+      // from n on: the last tile's unused tail, so the tile holds no match
+      return min((tt - I.t_first) * kTtTile + blk * 512 + L * 16 + __ffs(mL) - 1, I.n);
     }
   }
   return I.n;
@@ -365,6 +370,10 @@ __global__ void __launch_bounds__(kTtBThreads)
     reinterpret_cast<uint4*>(s_D)[tid] =
         reinterpret_cast<const uint4*>(S.D + (size_t)t * kTtTile)[tid];
   __syncthreads();
+  if (t0 + kTtTile > n) {  // the cloud's last tile: positions from n on are absent
+    for (int j = n - t0 + tid; j < kTtTile; j += kTtBThreads) s_D[j] = (uint8_t)kTtAbsent;
+    __syncthreads();
+  }
 
   const uint32_t below_me = (1u << lane) - 1u;
   const uint32_t above_me = ~below_me << 1;  // lanes > lane (lane 31: none)
@@ -441,7 +450,8 @@ __global__ void __launch_bounds__(kTtBThreads)
         } else {
           const uint4 w = *reinterpret_cast<const uint4*>(S.D + (size_t)(t + 1) * kTtTile);
           const uint32_t m = bytes_below(w, xv);
-          if (m) b = t0 + kTtTile + __ffs(m) - 1;
+          // a match from n on lies in the last tile's unused tail: none there
+          if (m) b = min(t0 + kTtTile + __ffs(m) - 1, n);
         }
       }
     }
@@ -495,6 +505,188 @@ __global__ void __launch_bounds__(kTtBThreads)
     for (int off = 16; off > 0; off >>= 1) own_sum += __shfl_xor_sync(kFull, own_sum, off);
     if (lane == 0 && own_sum != 0) atomicAdd(S.tile_sum + t, own_sum);
   }
+}
+
+// ------------------------------------------------------ unique + deltas --
+// Byte-wise minimum on the containing 32-bit word.
+__device__ void atomic_min_u8(uint8_t* addr, uint32_t v) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(addr) & ~uintptr_t(3));
+  const int sh = (int)(reinterpret_cast<uintptr_t>(addr) & 3) * 8;
+  uint32_t old = *reinterpret_cast<volatile uint32_t*>(w);
+  for (int it = 0; it < 4096; ++it) {  // retries only while other CTAs update the word
+    if (((old >> sh) & 0xffu) <= v) return;
+    const uint32_t assumed = old;
+    old = atomicCAS(w, assumed, (assumed & ~(0xffu << sh)) | (v << sh));
+    if (old == assumed) return;
+  }
+}
+
+constexpr int kUdThreads = 256;
+constexpr int kUdItems = kTtTile / kUdThreads;  // 16
+
+__device__ __forceinline__ int ud_pad(int j) { return j + (j >> 5); }
+
+// Run heads of sorted keys per 4,096-key tile; also resets the tree tiles'
+// edge-count sums and smallest deltas.
+__global__ void __launch_bounds__(kUdThreads)
+    unique_count_kernel(const uint32_t* __restrict__ keys, int n, TreeScratch S) {
+  __shared__ int s_cnt[kUdThreads / 32];
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const int start = t * kTtTile;
+  if (t == 0) {
+    const int pad = (int)align_up((size_t)S.tiles, kTtMinBlock);
+    for (int k = S.tiles + tid; k < pad; k += kUdThreads) S.tile_min[k] = (uint8_t)kTtAbsent;
+  }
+  if (tid == 0) {
+    S.tile_min[t] = (uint8_t)kTtAbsent;
+    S.tile_sum[t] = 0;
+  }
+  int cnt = 0;
+  const int j0 = start + tid * kUdItems;
+  if (j0 < n) {
+    uint32_t prev = j0 > 0 ? keys[j0 - 1] : 0u;
+    uint32_t k[kUdItems];
+    if (j0 + kUdItems <= n && (reinterpret_cast<uintptr_t>(keys + j0) & 15) == 0) {
+#pragma unroll
+      for (int q = 0; q < kUdItems / 4; ++q) {
+        const uint4 v = reinterpret_cast<const uint4*>(keys + j0)[q];
+        k[4 * q] = v.x;
+        k[4 * q + 1] = v.y;
+        k[4 * q + 2] = v.z;
+        k[4 * q + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < kUdItems; ++q) k[q] = j0 + q < n ? keys[j0 + q] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < kUdItems; ++q) {
+      if (j0 + q < n) {
+        cnt += (j0 + q == 0) || k[q] != prev;
+        prev = k[q];
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+  if ((tid & 31) == 0) s_cnt[tid >> 5] = cnt;
+  __syncthreads();
+  if (tid == 0) {
+    int total = 0;
+    for (int w = 0; w < kUdThreads / 32; ++w) total += s_cnt[w];
+    S.tile_heads[t] = total;
+  }
+}
+
+// Compaction from the tile prefixes; each unique code at output position o >= 1
+// also writes D[o - 1], the delta to the code before it (the last key of the
+// previous run), and the tiles' smallest deltas.
+__global__ void __launch_bounds__(kUdThreads)
+    unique_deltas_kernel(const uint32_t* __restrict__ keys, int n, uint32_t* __restrict__ out,
+                         TreeScratch S) {
+  __shared__ uint32_t s_keys[kTtTile + kTtTile / 32];
+  __shared__ uint8_t s_d[kTtTile];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  __shared__ uint32_t s_min[2][kUdThreads / 32];
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const int start = t * kTtTile;
+  const int valid = min(kTtTile, n - start);
+  if (valid <= 0) return;
+#pragma unroll 4
+  for (int j = tid; j < kTtTile; j += kUdThreads) {
+    const int idx = start + j;
+    s_keys[ud_pad(j)] = idx < n ? keys[idx] : 0u;
+  }
+  const uint32_t before = start > 0 ? keys[start - 1] : 0u;
+  __syncthreads();
+  uint32_t key[kUdItems], dk[kUdItems];
+  uint32_t flags = 0;
+  int cnt = 0;
+  const int j0 = tid * kUdItems;
+  uint32_t prev = j0 == 0 ? before : s_keys[ud_pad(j0 - 1)];
+#pragma unroll
+  for (int k = 0; k < kUdItems; ++k) {
+    key[k] = s_keys[ud_pad(j0 + k)];
+    const int j = j0 + k;
+    const bool head = j < valid && ((start + j == 0) || key[k] != prev);
+    dk[k] = tt_delta(prev, key[k]);  // used for heads past the first code only
+    flags |= (uint32_t)head << k;
+    cnt += head;
+    prev = key[k];
+  }
+  const uint32_t off = block_exclusive_sum<kUdThreads>((uint32_t)cnt, s_warp, &s_total);
+  const uint32_t total = s_total;
+  const uint32_t base = S.tile_upos[t];
+  // Stage the heads (s_keys is free after the scan's barriers) and their deltas.
+  uint32_t o = off;
+#pragma unroll
+  for (int k = 0; k < kUdItems; ++k) {
+    if (flags >> k & 1u) {
+      s_keys[ud_pad(o)] = key[k];
+      s_d[o] = (uint8_t)dk[k];
+      ++o;
+    }
+  }
+  __syncthreads();
+  // Deltas go to positions base - 1 .. base + total - 2 (the first code has none),
+  // i.e. tree tiles ta and at most ta + 1.
+  const int first = base == 0 ? 1 : 0;
+  const int ta = (int)(base + first - 1) / kTtTile;
+  uint32_t ma = kTtAbsent, mb = kTtAbsent;
+  for (int j = tid; j < (int)total; j += kUdThreads) {
+    out[base + j] = s_keys[ud_pad(j)];
+    if (j >= first) {
+      const int pos = (int)base + j - 1;
+      const uint32_t d = s_d[j];
+      S.D[pos] = (uint8_t)d;
+      if (pos / kTtTile == ta) ma = min(ma, d);
+      else mb = min(mb, d);
+    }
+  }
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) {
+    ma = min(ma, __shfl_xor_sync(kFull, ma, sh));
+    mb = min(mb, __shfl_xor_sync(kFull, mb, sh));
+  }
+  if ((tid & 31) == 0) {
+    s_min[0][tid >> 5] = ma;
+    s_min[1][tid >> 5] = mb;
+  }
+  __syncthreads();
+  if (tid == 0 && (int)total > first) {
+    uint32_t a = kTtAbsent, b = kTtAbsent;
+    for (int w = 0; w < kUdThreads / 32; ++w) {
+      a = min(a, s_min[0][w]);
+      b = min(b, s_min[1][w]);
+    }
+    if (a < kTtAbsent) atomic_min_u8(S.tile_min + ta, a);
+    if (b < kTtAbsent) atomic_min_u8(S.tile_min + ta + 1, b);
+  }
+}
+
+cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_out, int* d_unique,
+                                 void* tree_scratch, cudaStream_t s) {
+  if (n <= 0) return cudaMemsetAsync(d_unique, 0, sizeof(int), s);
+  const TreeScratch S = tree_scratch_carve(tree_scratch, n);
+  unique_count_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, n, S);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_tile_counts_scan(S.tiles, S.tile_heads, S.tile_upos, d_unique, s);
+  if (e != cudaSuccess) return e;
+  unique_deltas_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, n, codes_out, S);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_radix_tree_from_deltas(int n_host, const int* d_unique, const uint32_t* codes,
+                                          uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
+                                          int* left_child, int* parent, int* ec, void* scratch,
+                                          cudaStream_t s) {
+  if (n_host <= 0) return cudaSuccess;
+  const TreeScratch S = tree_scratch_carve(scratch, n_host);
+  const OneCloud map{n_host, d_unique, S.tiles};
+  const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
+  tree_nodes_kernel<<<S.tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint32_t* codes,
