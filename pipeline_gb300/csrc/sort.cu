@@ -580,7 +580,7 @@ cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float 
                           float range, const SortPlan* plan, void* ctrl, uint32_t* status,
                           cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int blocks = device_sm_count() * 4;
+  const int blocks = device_sm_count() * 6;
   long long need = (n + 255) / 256;
   const int grid = (int)(need < blocks ? need : blocks);
   if (plan) {
