@@ -435,7 +435,12 @@ __global__ void __launch_bounds__(kTtBThreads)
       else if (s_pl[c][xv] >= 0) a = t0 + s_pl[c][xv];
       if (nv != 0xFF) b = t0 + 32 * c + (int)nv;
       else if (s_sf[c][xv] < kTtTile) b = t0 + s_sf[c][xv];
-      if (a == -2) {  // the end of the previous tile first
+    }
+    // Neighbours outside the tile (the tile's running minima only): the edge
+    // of the adjacent tile first, then one warp-wide scan of the tile minima
+    // per query and of the found tile's deltas. Skipped by most chunks.
+    if (__any_sync(kFull, live && (a == -2 || b == -2))) {
+      if (live && a == -2) {
         if (t == I.t_first) {
           a = -1;
         } else {
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(kTtBThreads)
           if (m) a = t0 - 16 + 31 - __clz(m);
         }
       }
-      if (b == -2) {  // the start of the next tile first
+      if (live && b == -2) {
         if (t == I.t_last) {
           b = n;
         } else {
@@ -454,26 +459,24 @@ __global__ void __launch_bounds__(kTtBThreads)
           if (m) b = min(t0 + kTtTile + __ffs(m) - 1, n);
         }
       }
-    }
-    // Other tiles: one warp-wide scan of the tile minima per query, then of
-    // the found tile's deltas.
-    uint32_t need = __ballot_sync(kFull, live && a == -2);
-    while (need) {
-      const int src = __ffs(need) - 1;
-      need &= need - 1;
-      const uint32_t qx = __shfl_sync(kFull, xv, src);
-      const int tt = tiles_scan_left(S.tile_min, I.t_first, t - 1, qx, lane);
-      const int ans = tt >= 0 ? tile_last_below(S, I, tt, qx, lane) : -1;
-      if (lane == src) a = ans;
-    }
-    need = __ballot_sync(kFull, live && b == -2);
-    while (need) {
-      const int src = __ffs(need) - 1;
-      need &= need - 1;
-      const uint32_t qx = __shfl_sync(kFull, xv, src);
-      const int tt = tiles_scan_right(S.tile_min, t + 1, I.t_last, qx, lane);
-      const int ans = tt >= 0 ? tile_first_below(S, I, tt, qx, lane) : n;
-      if (lane == src) b = ans;
+      uint32_t need = __ballot_sync(kFull, live && a == -2);
+      while (need) {
+        const int src = __ffs(need) - 1;
+        need &= need - 1;
+        const uint32_t qx = __shfl_sync(kFull, xv, src);
+        const int tt = tiles_scan_left(S.tile_min, I.t_first, t - 1, qx, lane);
+        const int ans = tt >= 0 ? tile_last_below(S, I, tt, qx, lane) : -1;
+        if (lane == src) a = ans;
+      }
+      need = __ballot_sync(kFull, live && b == -2);
+      while (need) {
+        const int src = __ffs(need) - 1;
+        need &= need - 1;
+        const uint32_t qx = __shfl_sync(kFull, xv, src);
+        const int tt = tiles_scan_right(S.tile_min, t + 1, I.t_last, qx, lane);
+        const int ans = tt >= 0 ? tile_first_below(S, I, tt, qx, lane) : n;
+        if (lane == src) b = ans;
+      }
     }
     if (!live) continue;
     const int da = a < 0 ? -1 : (a >= t0 ? (int)s_D[a - t0] : (int)S.D[d_index(I, a)]);
