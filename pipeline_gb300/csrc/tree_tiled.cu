@@ -421,26 +421,28 @@ __global__ void __launch_bounds__(kTtBThreads)
   __syncwarp();
 
   int own_sum = 0;  // edge counts of this tile's nodes emitted here
+  // Per chunk, the common case without branches: both neighbours inside the
+  // tile (shared-memory tables); lanes needing another tile, the root or an
+  // edge count of another tile take warp-uniform guarded blocks.
 #pragma unroll 1
   for (int k = 0; k < kTtChunksPerWarp; ++k) {
     const int c = warp * kTtChunksPerWarp + k;
-    const int q = t0 + 32 * c + lane;
+    const int j = 32 * c + lane;
+    const int q = t0 + j;
     const bool live = q < n;
-    const uint32_t xv = s_D[32 * c + lane];
-    const uint32_t pv = s_pv[32 * c + lane], nv = s_nv[32 * c + lane];
+    const uint32_t xv = s_D[j];
+    const uint32_t pv = s_pv[j], nv = s_nv[j];
+    const int pl = s_pl[c][xv], sf = s_sf[c][xv];
     // -2: not in this tile
-    int a = -2, b = -2;
-    if (live) {
-      if (pv != 0xFF) a = t0 + 32 * c + (int)pv;
-      else if (s_pl[c][xv] >= 0) a = t0 + s_pl[c][xv];
-      if (nv != 0xFF) b = t0 + 32 * c + (int)nv;
-      else if (s_sf[c][xv] < kTtTile) b = t0 + s_sf[c][xv];
-    }
+    int a = pv != 0xFF ? t0 + 32 * c + (int)pv : (pl >= 0 ? t0 + pl : -2);
+    int b = nv != 0xFF ? t0 + 32 * c + (int)nv : (sf < kTtTile ? t0 + sf : -2);
+    int da = s_D[max(a - t0, 0)], db = s_D[min(max(b - t0, 0), kTtTile - 1)];
     // Neighbours outside the tile (the tile's running minima only): the edge
     // of the adjacent tile first, then one warp-wide scan of the tile minima
-    // per query and of the found tile's deltas. Skipped by most chunks.
+    // per query and of the found tile's deltas.
     if (__any_sync(kFull, live && (a == -2 || b == -2))) {
-      if (live && a == -2) {
+      const bool fa = live && a == -2, fb = live && b == -2;
+      if (fa) {
         if (t == I.t_first) {
           a = -1;
         } else {
@@ -449,7 +451,7 @@ __global__ void __launch_bounds__(kTtBThreads)
           if (m) a = t0 - 16 + 31 - __clz(m);
         }
       }
-      if (live && b == -2) {
+      if (fb) {
         if (t == I.t_last) {
           b = n;
         } else {
@@ -477,31 +479,38 @@ __global__ void __launch_bounds__(kTtBThreads)
         const int ans = tt >= 0 ? tile_first_below(S, I, tt, qx, lane) : n;
         if (lane == src) b = ans;
       }
+      if (fa && a >= 0) da = S.D[d_index(I, a)];
+      if (fb && b < n) db = S.D[d_index(I, b)];
     }
-    if (!live) continue;
-    const int da = a < 0 ? -1 : (a >= t0 ? (int)s_D[a - t0] : (int)S.D[d_index(I, a)]);
-    const int db = b >= n ? -1 : (b < t0 + kTtTile ? (int)s_D[b - t0] : (int)S.D[d_index(I, b)]);
-    if (a < 0 && b >= n) {  // the smallest delta overall
-      if (q <= n - 2) emit_root(o, n, q, xv, false);
-      continue;             // at n - 1: the root is short; node 0 comes from [0, n - 2]'s split
-    }
-    const int i = a < 0 ? b : (b >= n ? a + 1 : (da > db ? a + 1 : b));
-    const bool ll = a + 1 == q, lr = b == q + 1;
+    if (a < 0) da = -1;
+    if (b >= n) db = -1;
+    // a < 0 and b >= n: the smallest delta overall (the proper root), which
+    // gives radix node 0 unless it sits at n - 1 (a short root: node 0 then
+    // comes from the split of [0, n - 2], with a < 0 and b == n - 1).
+    const bool top = a < 0 && b >= n;
     const bool short_root = a < 0 && b == n - 1;
-    o.prefix_n[i] = (uint8_t)xv;
-    o.left_child[i] = q;
-    o.hll[i] = ll;
-    o.hlr[i] = lr;
-    if (!ll) o.parent[q] = i;
-    if (!lr) o.parent[q + 1] = i;
-    if (o.ec) {
-      const int e = short_root ? 0 : (int)(xv / 3) - max(da, db) / 3;
-      o.ec[i] = e;
-      const int ti = I.t_first + i / kTtTile;
-      if (ti == t) own_sum += e;
-      else atomicAdd(S.tile_sum + ti, e);
+    if (live && !top) {
+      const int i = a < 0 ? b : (b >= n ? a + 1 : (da > db ? a + 1 : b));
+      const bool ll = a + 1 == q, lr = b == q + 1;
+      o.prefix_n[i] = (uint8_t)xv;
+      o.left_child[i] = q;
+      o.hll[i] = ll;
+      o.hlr[i] = lr;
+      if (!ll) o.parent[q] = i;
+      if (!lr) o.parent[q + 1] = i;
+      if (o.ec) {
+        // the larger neighbour delta is the parent's (>= 0 whenever read)
+        const int e = short_root ? 0 : (int)(xv / 3u) - (int)((uint32_t)max(da, db) / 3u);
+        o.ec[i] = e;
+        const int ti = I.t_first + i / kTtTile;
+        own_sum += ti == t ? e : 0;
+        if (ti != t) atomicAdd(S.tile_sum + ti, e);
+      }
     }
-    if (short_root) emit_root(o, n, q, xv, true);
+    if (__any_sync(kFull, live && (top || short_root))) {
+      if (live && top && q <= n - 2) emit_root(o, n, q, xv, false);
+      if (live && short_root) emit_root(o, n, q, xv, true);
+    }
   }
   if (o.ec) {
 #pragma unroll
