@@ -385,11 +385,11 @@ __global__ void __launch_bounds__(kTtBThreads)
   for (int k = 0; k < kTtChunksPerWarp; ++k) {
     const int c = warp * kTtChunksPerWarp + k;
     const uint32_t d = s_D[32 * c + lane];
-    uint32_t b[5], dm[5];
+    uint32_t b[5];
     value_ballots(d, b);
-    bit_masks(d, dm);
-    const uint32_t lt_own = lanes_below(b, dm);
+    // lane v: the lanes whose delta is below v; a lane's own query is lane d's
     const uint32_t lt_lane = lanes_below(b, lm);
+    const uint32_t lt_own = __shfl_sync(kFull, lt_lane, (int)d);
     const uint32_t l = lt_own & below_me, r = lt_own & above_me;
     s_pv[32 * c + lane] = l ? (uint8_t)(31 - __clz(l)) : (uint8_t)0xFF;
     s_nv[32 * c + lane] = r ? (uint8_t)(__ffs(r) - 1) : (uint8_t)0xFF;
