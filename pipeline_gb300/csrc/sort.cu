@@ -218,15 +218,25 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
   if (STABLE) {
     uint16_t* wh = whist + warp * BINS;
     const uint32_t lt = lanemask_lt();
+    // Peers split the digit into a low and a high half of at most 5 bits:
+    // lane v builds the mask of lanes whose low (high) half equals v from the
+    // ballots of those bits, and a lane fetches the entries of its own halves.
+    constexpr int LOB = RB / 2, HIB = RB - LOB;
+    uint32_t lane_bits[HIB];  // all ones where the lane index has bit k
+#pragma unroll
+    for (int b = 0; b < HIB; ++b) lane_bits[b] = 0u - ((uint32_t)(lane >> b) & 1u);
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it) {
       const uint32_t d = (key[it] >> shift) & MASK;
-      uint32_t peers = 0xffffffffu;
+      uint32_t eq_lo = 0xffffffffu, eq_hi = 0xffffffffu;
 #pragma unroll
-      for (int b = 0; b < RB; ++b) {
-        const uint32_t bal = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-        peers &= ((d >> b) & 1u) ? bal : ~bal;
-      }
+      for (int b = 0; b < LOB; ++b)
+        eq_lo &= ~(__ballot_sync(0xffffffffu, (d >> b) & 1u) ^ lane_bits[b]);
+#pragma unroll
+      for (int b = 0; b < HIB; ++b)
+        eq_hi &= ~(__ballot_sync(0xffffffffu, (d >> (LOB + b)) & 1u) ^ lane_bits[b]);
+      const uint32_t peers = __shfl_sync(0xffffffffu, eq_lo, (int)(d & ((1u << LOB) - 1u))) &
+                             __shfl_sync(0xffffffffu, eq_hi, (int)(d >> LOB));
       const uint32_t before = wh[d];
       rank[it] = (uint16_t)(before + __popc(peers & lt));
       __syncwarp();
