@@ -275,6 +275,12 @@ __device__ uint32_t* bucket_radix_sort(uint32_t* a, uint32_t* b, int cnt, uint32
   // every warp takes `items` rows of 32 keys (the last warps may be partial)
   const int items = (cnt + kBkWarps * 32 - 1) / (kBkWarps * 32);
   const int seg = items * 32;
+  // peers from two 4-bit half-digit equality tables (lane v: lanes whose half
+  // equals v), fetched by shuffle
+  constexpr int kHalf = kRsBits / 2;
+  uint32_t lane_bits[kHalf];
+#pragma unroll
+  for (int b = 0; b < kHalf; ++b) lane_bits[b] = 0u - ((uint32_t)(lane >> b) & 1u);
   for (int shift = 0; shift < bits; shift += kRsBits) {
     for (int k = tid; k < kBkWarps * kRsBins / 2; k += kBkThreads)
       reinterpret_cast<uint32_t*>(S.whist)[k] = 0;
@@ -288,12 +294,15 @@ __device__ uint32_t* bucket_radix_sort(uint32_t* a, uint32_t* b, int cnt, uint32
       const bool valid = idx < cnt;
       const uint32_t key = valid ? a[idx] : 0u;
       const uint32_t dg = ((key - kmin) >> shift) & (kRsBins - 1);
-      uint32_t peers = __ballot_sync(0xffffffffu, valid);
+      uint32_t eq_lo = 0xffffffffu, eq_hi = 0xffffffffu;
 #pragma unroll
-      for (int bit = 0; bit < kRsBits; ++bit) {
-        const uint32_t bal = __ballot_sync(0xffffffffu, (dg >> bit) & 1u);
-        peers &= ((dg >> bit) & 1u) ? bal : ~bal;
+      for (int bit = 0; bit < kHalf; ++bit) {
+        eq_lo &= ~(__ballot_sync(0xffffffffu, (dg >> bit) & 1u) ^ lane_bits[bit]);
+        eq_hi &= ~(__ballot_sync(0xffffffffu, (dg >> (kHalf + bit)) & 1u) ^ lane_bits[bit]);
       }
+      const uint32_t peers = __ballot_sync(0xffffffffu, valid) &
+                             __shfl_sync(0xffffffffu, eq_lo, (int)(dg & ((1u << kHalf) - 1u))) &
+                             __shfl_sync(0xffffffffu, eq_hi, (int)(dg >> kHalf));
       const uint32_t before = valid ? wh[dg] : 0u;
       const uint32_t r = before + __popc(peers & lt);
       if (it & 1) rk[it >> 1] |= r << 16;
