@@ -613,13 +613,14 @@ LsortPlan lsort_plan(int n, int nb, int max_segments) {
     o = align_up(o + bytes, 256);
     return at;
   };
-  // zeroed each run:
+  // zeroed each run: everything up to the end of the fallback sort's zeroed
+  // part (its bases and per-tile histograms follow, written before use)
   p.stats_off = take(sizeof(LsortStats));
   p.counter_off = take(64);
   p.lookback_off = 0;  // unused: buckets publish counts, a scan packs them
-  p.sort_ctrl_off = take(p.fallback_sort.bytes);
   p.uniq_ctrl_off = take(p.fallback_unique.bytes);
-  p.zero_bytes = o;
+  p.sort_ctrl_off = take(p.fallback_sort.bytes);
+  p.zero_bytes = p.sort_ctrl_off + p.fallback_sort.zero_bytes;
   // not zeroed:
   p.hist_off = take(4 * (size_t)p.chunks * nb);
   p.totals_off = take(4 * (size_t)nb);

@@ -6,6 +6,30 @@
 
 namespace octgb {
 
+// Delta-based tree (csrc/tree_tiled.cu): tiles of 4,096 positions, whose
+// smallest deltas are scanned 512 at a time.
+constexpr int kTtTile = 4096;
+constexpr int kTtMinBlock = 512;
+// D of a position past the last one (and of malformed pairs): never below a
+// query value, which is at most 30 for codes below 2^31.
+constexpr uint32_t kTtAbsent = 31;
+__device__ __forceinline__ uint32_t tt_delta(uint32_t a, uint32_t b) {
+  return min((uint32_t)delta_u8(a, b), kTtAbsent);
+}
+
+// Byte-wise minimum on the containing 32-bit word.
+__device__ __forceinline__ void atomic_min_u8(uint8_t* addr, uint32_t v) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(addr) & ~uintptr_t(3));
+  const int sh = (int)(reinterpret_cast<uintptr_t>(addr) & 3) * 8;
+  uint32_t old = *reinterpret_cast<volatile uint32_t*>(w);
+  for (int it = 0; it < 4096; ++it) {  // retries only while other CTAs update the word
+    if (((old >> sh) & 0xffu) <= v) return;
+    const uint32_t assumed = old;
+    old = atomicCAS(w, assumed, (assumed & ~(0xffu << sh)) | (v << sh));
+    if (old == assumed) return;
+  }
+}
+
 // --------------------------------------------------------------------------
 // Karras radix tree (stage 4), one thread per node.
 // Replaces k_BuildRadixTree (include/kernels/04_radix_tree.hpp:5-11,

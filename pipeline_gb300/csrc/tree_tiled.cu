@@ -36,16 +36,11 @@
 
 namespace octgb {
 
-constexpr int kTtTile = 4096;
 constexpr int kTtChunks = kTtTile / 32;
 constexpr int kTtAThreads = 256;
 constexpr int kTtBThreads = 512;
 constexpr int kTtBWarps = kTtBThreads / 32;
 constexpr int kTtChunksPerWarp = kTtChunks / kTtBWarps;  // 8
-constexpr int kTtMinBlock = 512;  // tiles per step of the cross-tile scan (32 lanes x 16 bytes)
-// D of a position past the last one (and of malformed pairs): never below a
-// query value, which is at most 30 for codes below 2^31.
-constexpr uint32_t kTtAbsent = 31;
 constexpr uint32_t kFull = 0xffffffffu;
 
 static int tt_tiles(int n) { return ((n > 1 ? n : 1) + kTtTile - 1) / kTtTile; }
@@ -152,9 +147,6 @@ __device__ __forceinline__ void value_ballots(uint32_t d, uint32_t (&b)[5]) {
   for (int k = 0; k < 5; ++k) b[k] = __ballot_sync(kFull, (d >> k) & 1u);
 }
 
-__device__ __forceinline__ uint32_t tt_delta(uint32_t a, uint32_t b) {
-  return min((uint32_t)delta_u8(a, b), kTtAbsent);
-}
 
 template <class Map>
 __global__ void __launch_bounds__(kTtAThreads)
@@ -520,19 +512,6 @@ __global__ void __launch_bounds__(kTtBThreads)
 }
 
 // ------------------------------------------------------ unique + deltas --
-// Byte-wise minimum on the containing 32-bit word.
-__device__ void atomic_min_u8(uint8_t* addr, uint32_t v) {
-  uint32_t* w = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(addr) & ~uintptr_t(3));
-  const int sh = (int)(reinterpret_cast<uintptr_t>(addr) & 3) * 8;
-  uint32_t old = *reinterpret_cast<volatile uint32_t*>(w);
-  for (int it = 0; it < 4096; ++it) {  // retries only while other CTAs update the word
-    if (((old >> sh) & 0xffu) <= v) return;
-    const uint32_t assumed = old;
-    old = atomicCAS(w, assumed, (assumed & ~(0xffu << sh)) | (v << sh));
-    if (old == assumed) return;
-  }
-}
-
 constexpr int kUdThreads = 256;
 constexpr int kUdItems = kTtTile / kUdThreads;  // 16
 
