@@ -1,8 +1,11 @@
 // Stage 3 (unique) and stages 5-6 (edge count + inclusive prefix sum).
 //
-// Both are single-pass tile scans with decoupled look-back: a tile takes the
-// next id from an atomic counter, reduces its items, publishes its aggregate,
-// waits (bounded) for the inclusive prefix of the tiles before it and writes.
+// The stage entry points are single-pass tile scans with decoupled look-back:
+// a tile takes the next id from an atomic counter, reduces its items,
+// publishes its aggregate, waits (bounded) for the inclusive prefix of the
+// tiles before it and writes. The whole builds take the tile prefixes from a
+// scan of per-tile sums made earlier (run heads: csrc/tree_tiled.cu; edge
+// counts: the tree kernel), so their tiles never wait on one another.
 //
 // Unique replaces k_CountUnique (reference include/kernels/03_unique.hpp:4,
 // kernels/03_unique.cpp:2-16; the reference GPU form is one thread,

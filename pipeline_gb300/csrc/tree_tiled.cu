@@ -21,15 +21,22 @@
 // delta, so the edge count prefix_n[i]/3 - prefix_n[parent[i]]/3
 // (kernels/05_edge_count.cpp:3-16) is computed here as well.
 //
-// Two kernels over tiles of 4,096 positions:
-//   tree_tiles_kernel  D as bytes and each tile's smallest D;
-//   tree_nodes_kernel  nearest smaller deltas inside each 32-position chunk
-//                      from five ballots over the bits of D, across the
-//                      tile's chunks from prefix / suffix tables in shared
-//                      memory, across tiles (rare: only the tile's running
-//                      minima) by a warp-wide scan of the tile minima and then
-//                      of the found tile's deltas; then every output of the
-//                      node split at each position.
+// Kernels over tiles of 4,096 positions:
+//   tree_tiles_kernel     D as bytes and each tile's smallest D, from the
+//                         codes (learned and batched builds, the C entry);
+//   unique_count_kernel,  the whole build's stage 3: run heads of the sorted
+//   unique_deltas_kernel  keys counted per tile and scanned, then compacted,
+//                         each unique code also writing D for the code before
+//                         it and the tiles' smallest D;
+//   tree_nodes_kernel     nearest smaller deltas inside each 32-position
+//                         chunk from five ballots over the bits of D (one
+//                         lane-parallel table of masks per chunk), across the
+//                         tile's chunks from prefix / suffix tables in shared
+//                         memory, across tiles (rare: only the tile's running
+//                         minima) by a peek at the adjacent tile's edge, then
+//                         warp-wide scans of the tile minima and of the found
+//                         tile's deltas; then every output of the node split
+//                         at each position.
 #include <climits>
 
 #include "tree.cuh"
