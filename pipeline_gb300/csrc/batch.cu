@@ -11,9 +11,12 @@
 //   sort      reduce-then-scan radix passes: per-tile digit histograms, a
 //             per-cloud tile-prefix scan, and the pass kernel driven by tile
 //             descriptors (cloud-local positions are absolute indices);
-//   unique    decoupled look-back chains that restart at each cloud's first
-//             tile; tiles come from an atomic work queue;
-//   tree      the single-cloud delta kernels over the same 4,096-position
+//   unique    the single-cloud run-head count, one scan of all tiles' counts
+//             (a tile's offset is its entry minus that of its cloud's first
+//             tile) and the compaction that also writes each code's delta to
+//             the one before it into the cloud's tree tiles, and each cloud's
+//             U from its last tile;
+//   tree      the single-cloud tree_nodes kernel over the same 4,096-position
 //             tiles (tile map: cloud, cloud start, the cloud's tile range),
 //             writing the edge counts and their per-tile sums;
 //   scan      one scan of the tile sums for all clouds; a tile's prefix is its
@@ -184,114 +187,6 @@ __global__ void __launch_bounds__(32 * kTsGroups)
     const uint32_t v = th[(size_t)t * bins + d];
     th[(size_t)t * bins + d] = run;
     run += v;
-  }
-}
-
-// ------------------------------------------------------ look-back chains --
-constexpr unsigned long long kBAgg = 1ull << 62;
-constexpr unsigned long long kBInc = 2ull << 62;
-constexpr unsigned long long kBFlags = 3ull << 62;
-
-// Warp look-back whose chain starts at tile `first` (the cloud's first tile).
-__device__ uint32_t chain_lookback(unsigned long long* lb, int tile, int first, uint32_t agg,
-                                   uint32_t* status) {
-  const int lane = threadIdx.x & 31;
-  if (tile == first) {
-    if (lane == 0) st_release_u64(lb + tile, kBInc | agg);
-    return 0;
-  }
-  if (lane == 0) st_release_u64(lb + tile, kBAgg | agg);
-  uint32_t ex = 0;
-  int pred = tile - 1;
-  uint32_t spins = 0;
-  while (true) {
-    const int p = pred - lane;
-    const unsigned long long w = p >= first ? ld_relaxed_u64(lb + p) : kBInc;
-    const unsigned long long f = w & kBFlags;
-    const uint32_t inc_m = __ballot_sync(0xffffffffu, f == kBInc);
-    const uint32_t nr_m = __ballot_sync(0xffffffffu, f == 0);
-    const int first_inc = inc_m ? __ffs(inc_m) - 1 : 32;
-    const int first_nr = nr_m ? __ffs(nr_m) - 1 : 32;
-    if (first_nr < first_inc) {
-      ex += __reduce_add_sync(0xffffffffu, lane < first_nr ? (uint32_t)w : 0u);
-      pred -= first_nr;
-      if (++spins > kSpinLimit) {
-        if (lane == 0) raise_status(status, kStatusSpinTimeout);
-        break;
-      }
-      backoff(spins);
-      continue;
-    }
-    const int take = first_inc < 32 ? first_inc + 1 : 32;
-    ex += __reduce_add_sync(0xffffffffu, lane < take ? (uint32_t)w : 0u);
-    if (first_inc < 32) break;
-    pred -= 32;
-  }
-  if (lane == 0) st_release_u64(lb + tile, kBInc | (uint32_t)(ex + agg));
-  return ex;
-}
-
-__device__ __forceinline__ bool last_tile_of_cloud(const BatchDev& B, int t) {
-  return t == B.T4 - 1 || B.tiles4k[t + 1].z != B.tiles4k[t].z;
-}
-
-// ----------------------------------------------------------------- unique --
-constexpr int kBuThreads = 256;
-constexpr int kBuItems = 16;
-static_assert(kBuThreads * kBuItems == kBatchTile4k, "unique tile");
-
-__device__ __forceinline__ int pad_idx4k(int j) { return j + (j >> 5); }
-
-__global__ void __launch_bounds__(kBuThreads)
-    batch_unique_kernel(const uint32_t* src, uint32_t* dst, BatchDev B, int* __restrict__ unique_c,
-                        unsigned long long* __restrict__ lb, uint32_t* __restrict__ queue,
-                        uint32_t* __restrict__ status) {
-  __shared__ uint32_t s_keys[kBatchTile4k + kBatchTile4k / 32];
-  __shared__ uint32_t s_warp[32];
-  __shared__ uint32_t s_misc[4];
-  const int tid = threadIdx.x;
-  while (true) {
-    if (tid == 0) s_misc[0] = atomicAdd(queue, 1u);
-    __syncthreads();
-    const int t = (int)s_misc[0];
-    if (t >= B.T4) return;
-    const int4 d = B.tiles4k[t];
-    const int start = d.x, valid = d.y - d.x, c = d.z;
-    const int cs = B.start[c];
-#pragma unroll 4
-    for (int j = tid; j < kBatchTile4k; j += kBuThreads)
-      s_keys[pad_idx4k(j)] = j < valid ? src[start + j] : 0u;
-    if (tid == 0) s_misc[1] = start > cs ? src[start - 1] : 0u;
-    __syncthreads();
-    uint32_t key[kBuItems];
-    uint32_t flags = 0;
-    int cnt = 0;
-    const int j0 = tid * kBuItems;
-    uint32_t prev = j0 == 0 ? s_misc[1] : s_keys[pad_idx4k(j0 - 1)];
-#pragma unroll
-    for (int k = 0; k < kBuItems; ++k) {
-      key[k] = s_keys[pad_idx4k(j0 + k)];
-      const int j = j0 + k;
-      const bool head = j < valid && ((start + j == cs) || key[k] != prev);
-      flags |= (uint32_t)head << k;
-      cnt += head;
-      prev = key[k];
-    }
-    const uint32_t off = block_exclusive_sum<kBuThreads>((uint32_t)cnt, s_warp, &s_misc[2]);
-    const uint32_t total = s_misc[2];
-    if (tid < 32) {
-      const uint32_t e = chain_lookback(lb, t, d.w, total, status);
-      if (tid == 0) s_misc[3] = e;
-    }
-    uint32_t o = off;
-#pragma unroll
-    for (int k = 0; k < kBuItems; ++k)
-      if (flags >> k & 1u) s_keys[pad_idx4k(o++)] = key[k];
-    __syncthreads();
-    const uint32_t ex = s_misc[3];
-    for (int j = tid; j < (int)total; j += kBuThreads) dst[cs + ex + j] = s_keys[pad_idx4k(j)];
-    if (tid == 0 && last_tile_of_cloud(B, t)) unique_c[c] = (int)(ex + total);
-    __syncthreads();
   }
 }
 
@@ -501,7 +396,7 @@ struct oct_batch_plan {
   size_t t_start = 0, t_node_start = 0, t_tile0 = 0, t_sort = 0, t_4k = 0, t_slots = 0,
          tables_bytes = 0;
   // workspace offsets
-  size_t w_status = 0, w_unique = 0, w_maxslot = 0, w_hist = 0, w_queues = 0, w_lb_u = 0,
+  size_t w_status = 0, w_unique = 0, w_maxslot = 0, w_hist = 0,
          zero_bytes = 0, w_tree = 0, w_base = 0, w_th = 0, w_keys_a = 0, w_keys_b = 0,
          w_tags = 0, ws_bytes = 0;
 };
@@ -605,8 +500,6 @@ OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_siz
   P->w_unique = take(4 * (size_t)n_clouds);
   P->w_maxslot = take(4 * (size_t)n_clouds);
   P->w_hist = take(4 * (size_t)n_clouds * passes * bins);
-  P->w_queues = take(64);
-  P->w_lb_u = take(8 * (P->tiles4k.size() + 1));
   P->zero_bytes = o;
   P->w_tree = take(tree_scratch_bytes_tiles((int)P->tiles4k.size()));
   P->w_base = take(4 * (size_t)n_clouds * passes * bins);
@@ -679,8 +572,6 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
   int* unique_c = reinterpret_cast<int*>(w + P->w_unique);
   int* max_slot_c = reinterpret_cast<int*>(w + P->w_maxslot);
   uint32_t* hist = reinterpret_cast<uint32_t*>(w + P->w_hist);
-  uint32_t* queues = reinterpret_cast<uint32_t*>(w + P->w_queues);
-  unsigned long long* lb_u = reinterpret_cast<unsigned long long*>(w + P->w_lb_u);
   uint32_t* base = reinterpret_cast<uint32_t*>(w + P->w_base);
   uint32_t* th = reinterpret_cast<uint32_t*>(w + P->w_th);
   uint32_t* ka = reinterpret_cast<uint32_t*>(w + P->w_keys_a);
@@ -717,15 +608,14 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
       b = t;
     }
     if (e != cudaSuccess) return batch_fail(e, "batch: sort");
-    const int qgrid = std::max(1, std::min(B.T4, sms * 8));
-    batch_unique_kernel<<<qgrid, kBuThreads, 0, s>>>(a, out->codes, B, unique_c, lb_u, queues,
-                                                     status);
     void* tree_ws = w + P->w_tree;
     const TreeScratch TS = tree_scratch_carve_tiles(tree_ws, B.T4);
-    e = launch_batch_radix_tree(B.tiles4k, B.T4, B.start, unique_c, out->codes,
-                                out->tree.prefix_n, out->tree.has_leaf_left,
-                                out->tree.has_leaf_right, out->tree.left_child, out->tree.parent,
-                                out->edge_count, tree_ws, s);
+    e = launch_batch_unique_deltas(a, B.tiles4k, B.T4, B.start, out->codes, unique_c, tree_ws, s);
+    if (e == cudaSuccess)
+      e = launch_batch_radix_tree_from_deltas(B.tiles4k, B.T4, B.start, unique_c, out->codes,
+                                              out->tree.prefix_n, out->tree.has_leaf_left,
+                                              out->tree.has_leaf_right, out->tree.left_child,
+                                              out->tree.parent, out->edge_count, tree_ws, s);
     if (e == cudaSuccess) e = launch_tile_sums_scan(B.T4, TS.tile_sum, TS.tile_prefix, s);
     if (e != cudaSuccess) return batch_fail(e, "batch: tree");
     const OctTags tags = oct_tags_carve(w + P->w_tags, std::max(P->total_cap, 1));

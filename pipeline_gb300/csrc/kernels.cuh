@@ -130,6 +130,17 @@ TreeScratch tree_scratch_carve(void* base, int n_host);
 // tiles' smallest deltas), so only tree_nodes_kernel remains of stage 4.
 cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_out, int* d_unique,
                                  void* tree_scratch, cudaStream_t s);
+// The same for batched clouds over their 4,096-key tiles (descriptors
+// {first, end, cloud, first tile of cloud}): each cloud's codes from its
+// start, its U to unique_c[cloud], its deltas in its own tree tiles.
+cudaError_t launch_batch_unique_deltas(const uint32_t* sorted, const int4* tiles, int n_tiles,
+                                       const int* start, uint32_t* codes_out, int* unique_c,
+                                       void* scratch, cudaStream_t s);
+cudaError_t launch_batch_radix_tree_from_deltas(const int4* tiles, int n_tiles, const int* start,
+                                                const int* unique_c, const uint32_t* codes,
+                                                uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
+                                                int* left_child, int* parent, int* ec,
+                                                void* scratch, cudaStream_t s);
 // The radix tree (and edge counts) from deltas already in the scratch.
 cudaError_t launch_radix_tree_from_deltas(int n_host, const int* d_unique, const uint32_t* codes,
                                           uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,

@@ -23,11 +23,13 @@
 //
 // Kernels over tiles of 4,096 positions:
 //   tree_tiles_kernel     D as bytes and each tile's smallest D, from the
-//                         codes (learned and batched builds, the C entry);
-//   unique_count_kernel,  the whole build's stage 3: run heads of the sorted
-//   unique_deltas_kernel  keys counted per tile and scanned, then compacted,
-//                         each unique code also writing D for the code before
-//                         it and the tiles' smallest D;
+//                         codes (learned build, the C entry);
+//   unique_count_kernel,  stage 3 of the whole and batched builds: run heads
+//   unique_deltas_kernel  of the sorted keys counted per tile and scanned,
+//                         then compacted, each unique code also writing D for
+//                         the code before it and the tiles' smallest D (per
+//                         cloud in the batched build: tile maps OneKeys /
+//                         CloudKeys);
 //   tree_nodes_kernel     nearest smaller deltas inside each 32-position
 //                         chunk from five ballots over the bits of D (one
 //                         lane-parallel table of masks per chunk), across the
@@ -524,13 +526,54 @@ constexpr int kUdItems = kTtTile / kUdThreads;  // 16
 
 __device__ __forceinline__ int ud_pad(int j) { return j + (j >> 5); }
 
-// Run heads of sorted keys per 4,096-key tile; also resets the tree tiles'
-// edge-count sums and smallest deltas.
+// A 4,096-key tile of sorted keys: keys [lo, hi) of the cloud starting at cs,
+// whose unique codes go to the tree tiles from t_first on.
+struct KeyTile {
+  int lo, hi, cs, t_first, cloud;
+  bool last;  // the cloud's last tile
+};
+
+// One cloud of n keys.
+struct OneKeys {
+  int n;
+  __device__ __forceinline__ KeyTile operator()(int t) const {
+    KeyTile K;
+    K.lo = t * kTtTile;
+    K.hi = min(K.lo + kTtTile, n);
+    K.cs = 0;
+    K.t_first = 0;
+    K.cloud = 0;
+    K.last = K.hi >= n;
+    return K;
+  }
+};
+
+// Batched clouds: tile descriptors {first, end, cloud, first tile of cloud}.
+struct CloudKeys {
+  const int4* tiles;
+  int n_tiles;
+  const int* start;
+  __device__ __forceinline__ KeyTile operator()(int t) const {
+    const int4 d = tiles[t];
+    KeyTile K;
+    K.lo = d.x;
+    K.hi = d.y;
+    K.cs = start[d.z];
+    K.t_first = d.w;
+    K.cloud = d.z;
+    K.last = t == n_tiles - 1 || tiles[t + 1].z != d.z;
+    return K;
+  }
+};
+
+// Run heads of sorted keys per tile; also resets the tree tiles' edge-count
+// sums and smallest deltas.
+template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
-    unique_count_kernel(const uint32_t* __restrict__ keys, int n, TreeScratch S) {
+    unique_count_kernel(const uint32_t* __restrict__ keys, Map map, TreeScratch S) {
   __shared__ int s_cnt[kUdThreads / 32];
   const int t = blockIdx.x, tid = threadIdx.x;
-  const int start = t * kTtTile;
+  const KeyTile K = map(t);
   if (t == 0) {
     const int pad = (int)align_up((size_t)S.tiles, kTtMinBlock);
     for (int k = S.tiles + tid; k < pad; k += kUdThreads) S.tile_min[k] = (uint8_t)kTtAbsent;
@@ -540,11 +583,11 @@ __global__ void __launch_bounds__(kUdThreads)
     S.tile_sum[t] = 0;
   }
   int cnt = 0;
-  const int j0 = start + tid * kUdItems;
-  if (j0 < n) {
-    uint32_t prev = j0 > 0 ? keys[j0 - 1] : 0u;
+  const int j0 = K.lo + tid * kUdItems;
+  if (j0 < K.hi) {
+    uint32_t prev = j0 > K.cs ? keys[j0 - 1] : 0u;
     uint32_t k[kUdItems];
-    if (j0 + kUdItems <= n && (reinterpret_cast<uintptr_t>(keys + j0) & 15) == 0) {
+    if (j0 + kUdItems <= K.hi && (reinterpret_cast<uintptr_t>(keys + j0) & 15) == 0) {
 #pragma unroll
       for (int q = 0; q < kUdItems / 4; ++q) {
         const uint4 v = reinterpret_cast<const uint4*>(keys + j0)[q];
@@ -555,12 +598,12 @@ __global__ void __launch_bounds__(kUdThreads)
       }
     } else {
 #pragma unroll
-      for (int q = 0; q < kUdItems; ++q) k[q] = j0 + q < n ? keys[j0 + q] : 0u;
+      for (int q = 0; q < kUdItems; ++q) k[q] = j0 + q < K.hi ? keys[j0 + q] : 0u;
     }
 #pragma unroll
     for (int q = 0; q < kUdItems; ++q) {
-      if (j0 + q < n) {
-        cnt += (j0 + q == 0) || k[q] != prev;
+      if (j0 + q < K.hi) {
+        cnt += (j0 + q == K.cs) || k[q] != prev;
         prev = k[q];
       }
     }
@@ -576,27 +619,29 @@ __global__ void __launch_bounds__(kUdThreads)
   }
 }
 
-// Compaction from the tile prefixes; each unique code at output position o >= 1
-// also writes D[o - 1], the delta to the code before it (the last key of the
-// previous run), and the tiles' smallest deltas.
+// Compaction from the tile prefixes; each unique code at (cloud) position
+// o >= 1 also writes D[o - 1], the delta to the code before it (the last key
+// of the previous run), and the tiles' smallest deltas. With unique_c, each
+// cloud's last tile writes the cloud's U.
+template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
-    unique_deltas_kernel(const uint32_t* __restrict__ keys, int n, uint32_t* __restrict__ out,
-                         TreeScratch S) {
+    unique_deltas_kernel(const uint32_t* __restrict__ keys, Map map, uint32_t* __restrict__ out,
+                         TreeScratch S, int* __restrict__ unique_c) {
   __shared__ uint32_t s_keys[kTtTile + kTtTile / 32];
   __shared__ uint8_t s_d[kTtTile];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ uint32_t s_min[2][kUdThreads / 32];
   const int t = blockIdx.x, tid = threadIdx.x;
-  const int start = t * kTtTile;
-  const int valid = min(kTtTile, n - start);
+  const KeyTile K = map(t);
+  const int valid = K.hi - K.lo;
   if (valid <= 0) return;
 #pragma unroll 4
   for (int j = tid; j < kTtTile; j += kUdThreads) {
-    const int idx = start + j;
-    s_keys[ud_pad(j)] = idx < n ? keys[idx] : 0u;
+    const int idx = K.lo + j;
+    s_keys[ud_pad(j)] = j < valid ? keys[idx] : 0u;
   }
-  const uint32_t before = start > 0 ? keys[start - 1] : 0u;
+  const uint32_t before = K.lo > K.cs ? keys[K.lo - 1] : 0u;
   __syncthreads();
   uint32_t key[kUdItems], dk[kUdItems];
   uint32_t flags = 0;
@@ -607,15 +652,15 @@ __global__ void __launch_bounds__(kUdThreads)
   for (int k = 0; k < kUdItems; ++k) {
     key[k] = s_keys[ud_pad(j0 + k)];
     const int j = j0 + k;
-    const bool head = j < valid && ((start + j == 0) || key[k] != prev);
-    dk[k] = tt_delta(prev, key[k]);  // used for heads past the first code only
+    const bool head = j < valid && ((K.lo + j == K.cs) || key[k] != prev);
+    dk[k] = tt_delta(prev, key[k]);  // used for heads past the cloud's first code only
     flags |= (uint32_t)head << k;
     cnt += head;
     prev = key[k];
   }
   const uint32_t off = block_exclusive_sum<kUdThreads>((uint32_t)cnt, s_warp, &s_total);
   const uint32_t total = s_total;
-  const uint32_t base = S.tile_upos[t];
+  const uint32_t base = S.tile_upos[t] - S.tile_upos[K.t_first];
   // Stage the heads (s_keys is free after the scan's barriers) and their deltas.
   uint32_t o = off;
 #pragma unroll
@@ -627,17 +672,17 @@ __global__ void __launch_bounds__(kUdThreads)
     }
   }
   __syncthreads();
-  // Deltas go to positions base - 1 .. base + total - 2 (the first code has none),
-  // i.e. tree tiles ta and at most ta + 1.
+  // Deltas go to positions base - 1 .. base + total - 2 (the cloud's first code
+  // has none), i.e. the cloud's tree tiles ta and at most ta + 1.
   const int first = base == 0 ? 1 : 0;
   const int ta = (int)(base + first - 1) / kTtTile;
   uint32_t ma = kTtAbsent, mb = kTtAbsent;
   for (int j = tid; j < (int)total; j += kUdThreads) {
-    out[base + j] = s_keys[ud_pad(j)];
+    out[K.cs + base + j] = s_keys[ud_pad(j)];
     if (j >= first) {
       const int pos = (int)base + j - 1;
       const uint32_t d = s_d[j];
-      S.D[pos] = (uint8_t)d;
+      S.D[(size_t)(K.t_first + pos / kTtTile) * kTtTile + pos % kTtTile] = (uint8_t)d;
       if (pos / kTtTile == ta) ma = min(ma, d);
       else mb = min(mb, d);
     }
@@ -652,14 +697,17 @@ __global__ void __launch_bounds__(kUdThreads)
     s_min[1][tid >> 5] = mb;
   }
   __syncthreads();
-  if (tid == 0 && (int)total > first) {
-    uint32_t a = kTtAbsent, b = kTtAbsent;
-    for (int w = 0; w < kUdThreads / 32; ++w) {
-      a = min(a, s_min[0][w]);
-      b = min(b, s_min[1][w]);
+  if (tid == 0) {
+    if ((int)total > first) {
+      uint32_t a = kTtAbsent, b = kTtAbsent;
+      for (int w = 0; w < kUdThreads / 32; ++w) {
+        a = min(a, s_min[0][w]);
+        b = min(b, s_min[1][w]);
+      }
+      if (a < kTtAbsent) atomic_min_u8(S.tile_min + K.t_first + ta, a);
+      if (b < kTtAbsent) atomic_min_u8(S.tile_min + K.t_first + ta + 1, b);
     }
-    if (a < kTtAbsent) atomic_min_u8(S.tile_min + ta, a);
-    if (b < kTtAbsent) atomic_min_u8(S.tile_min + ta + 1, b);
+    if (unique_c && K.last) unique_c[K.cloud] = (int)(base + total);
   }
 }
 
@@ -667,11 +715,39 @@ cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_
                                  void* tree_scratch, cudaStream_t s) {
   if (n <= 0) return cudaMemsetAsync(d_unique, 0, sizeof(int), s);
   const TreeScratch S = tree_scratch_carve(tree_scratch, n);
-  unique_count_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, n, S);
+  const OneKeys map{n};
+  unique_count_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, S);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = launch_tile_counts_scan(S.tiles, S.tile_heads, S.tile_upos, d_unique, s);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, n, codes_out, S);
+  unique_deltas_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_unique_deltas(const uint32_t* sorted, const int4* tiles, int n_tiles,
+                                       const int* start, uint32_t* codes_out, int* unique_c,
+                                       void* scratch, cudaStream_t s) {
+  if (n_tiles <= 0) return cudaSuccess;
+  const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
+  const CloudKeys map{tiles, n_tiles, start};
+  unique_count_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, S);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_tile_counts_scan(n_tiles, S.tile_heads, S.tile_upos, nullptr, s);
+  if (e != cudaSuccess) return e;
+  unique_deltas_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, unique_c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_radix_tree_from_deltas(const int4* tiles, int n_tiles, const int* start,
+                                                const int* unique_c, const uint32_t* codes,
+                                                uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
+                                                int* left_child, int* parent, int* ec,
+                                                void* scratch, cudaStream_t s) {
+  if (n_tiles <= 0) return cudaSuccess;
+  const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
+  const CloudTiles map{tiles, start, unique_c};
+  const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
+  tree_nodes_kernel<<<n_tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
   return cudaGetLastError();
 }
 
