@@ -56,18 +56,23 @@ WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 
 # as fixed by the octree-build analysis: stage 1 reads 16 B and writes 4 B per
 # point (its digit histograms are fused, so the sort reads no extra 4 B/key);
 # each 10-bit sort pass reads and writes 4 B per key; unique reads 4 B per key
-# and writes 4 B per unique key; the radix tree with its edge counts reads 4 B
+# and writes 4 B per unique key (in the MSD form of large even clouds: one
+# scatter pass of 8 B per key, the bucket bitmaps reading 4 B per key and
+# writing 4 B per unique key, and the pack reading 4 B and writing 5 B per
+# unique key: code and delta); the radix tree with its edge counts reads 4 B
 # per code and writes 15 B per node (11 B of tree + 4 B of edge count); the
 # prefix sum reads 4 B and writes 4 B per node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
 # leaf link (split over the emit and finalize launches).
-def algorithmic_bytes(n, u, b, m):
+def algorithmic_bytes(n, u, b, m, msd=False):
     leaves = b + 1
+    if msd:  # MSD form: one scatter pass, bucket bitmaps, pack (codes + deltas)
+        sort = {"msd scatter": 8 * n, "msd buckets": 4 * n + 4 * u, "unique": 9 * u}
+    else:
+        sort = {"sort pass 0": 8 * n, "sort pass 1": 8 * n, "sort pass 2": 8 * n,
+                "unique": 4 * n + 4 * u}
     return {
         "morton+histogram": 20 * n,
-        "sort pass 0": 8 * n,
-        "sort pass 1": 8 * n,
-        "sort pass 2": 8 * n,
-        "unique": 4 * n + 4 * u,
+        **sort,
         "radix tree+edge count": 4 * u + 15 * b,
         "prefix sum": 8 * b,
         "octree emit": 40 * b + 4 * leaves,
@@ -293,7 +298,10 @@ def run_ours(args, rank, world, local_rank):
     per_kernel = {}
     for i in range(1, nsteps):
         per_kernel[names[i]] = statistics.median(evs[r][i - 1].elapsed_time(evs[r][i]) for r in range(reps))
-    alg = algorithmic_bytes(n, u, b, m)
+    # the MSD form ran when its bucket stage did work (its kernels otherwise
+    # return at once)
+    msd_form = per_kernel.get("msd buckets", 0.0) > 0.005
+    alg = algorithmic_bytes(n, u, b, m, msd_form)
     hbm_peak, peak_kind = peaks()
     stages = {}
     for name, t in per_kernel.items():
@@ -387,7 +395,7 @@ def run_ours(args, rank, world, local_rank):
     base = None
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(pts_h)
-    launches_per_step = build_launches()
+    launches_per_step = build_launches(n)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4),
@@ -453,7 +461,7 @@ def host_link_bound(dev, pinned_in, pinned_out, in_bytes: int, out_bytes: int) -
             "both_ms": round(both_ms, 4), "both_gbs": round((in_bytes + out_bytes) / both_ms / 1e6, 1)}
 
 
-def build_launches() -> int:
+def build_launches(n: int = 0) -> int:
     """Kernel launches of one plain build under the active sort shape:
     Morton, digit-base scan, per pass (tile histogram + tile scan +) pass,
     unique (run-head count, their scan, compaction with the deltas), tree
@@ -463,7 +471,11 @@ def build_launches() -> int:
 
     rb, _, _, scan = autotune.get_config()
     passes = (30 + rb - 1) // rb
-    return 2 + passes * (3 if scan == 1 else 1) + 3 + 1 + 2 + 2 + 1
+    lsd = 2 + passes * (3 if scan == 1 else 1) + 3 + 1 + 2 + 2 + 1
+    # MSD form (launched beside the LSD passes for clouds of 2^22+ points):
+    # form gate, top-digit scatter (3), bucket bitmaps, pack scan + pack
+    msd = 7 if (n >= (1 << 22) and rb == 10 and passes == 3 and scan == 1) else 0
+    return lsd + msd
 
 
 def profile_only(args):

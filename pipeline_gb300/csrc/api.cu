@@ -33,7 +33,7 @@ struct BuildLayout {
   SortPlan sort;
   ScanPlan uniq;
   size_t sort_off, uniq_off, misc_off, ctrl_bytes;
-  size_t keys_a_off, keys_b_off, tree_off, tags_off, total;
+  size_t msd_off, keys_a_off, keys_b_off, tree_off, tags_off, total;
 };
 
 BuildLayout build_layout(int n, int cap) {
@@ -47,7 +47,8 @@ BuildLayout build_layout(int n, int cap) {
   L.misc_off = align_up(L.uniq_off + L.uniq.bytes, 256);
   L.sort_off = align_up(L.misc_off + 256, 256);
   L.ctrl_bytes = L.sort_off + L.sort.zero_bytes;
-  L.keys_a_off = align_up(L.sort_off + L.sort.bytes, 256);
+  L.msd_off = align_up(L.sort_off + L.sort.bytes, 256);
+  L.keys_a_off = align_up(L.msd_off + msd_scratch_bytes(), 256);
   L.keys_b_off = align_up(L.keys_a_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
   L.tree_off = align_up(L.keys_b_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
   L.tags_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
@@ -55,17 +56,20 @@ BuildLayout build_layout(int n, int cap) {
   return L;
 }
 
-// misc area: [0] status, [1] n_unique, [2] max octree slot
+// misc area: [0] status, [1] n_unique, [2] max octree slot, [4..5] sort form
+// flags (MSD, LSD)
 struct Misc {
   uint32_t* status;
   int* unique;
   int* max_slot;
+  uint32_t* form;
 };
 Misc misc_at(char* base) {
   Misc m;
   m.status = reinterpret_cast<uint32_t*>(base);
   m.unique = reinterpret_cast<int*>(base + 4);
   m.max_slot = reinterpret_cast<int*>(base + 8);
+  m.form = reinterpret_cast<uint32_t*>(base + 16);
   return m;
 }
 
@@ -367,13 +371,40 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
                         &L.sort, w + L.sort_off, m.status, s),
           "build: morton");
   mark(rec, s);
+  // Stages 2-3: LSD passes + run-head unique, or for large even clouds the
+  // MSD form (top-digit scatter, per-bucket bitmaps, pack), chosen on the
+  // device from the top-digit histogram; both write the sorted unique codes,
+  // U and the deltas of adjacent codes, from which the tree (with the edge
+  // counts) is built.
+  const bool msd = n >= msd_min_n() && msd_plan_ok(L.sort);
+  char* sort_ctrl = w + L.sort_off;
+  const uint32_t* top_hist = reinterpret_cast<const uint32_t*>(sort_ctrl + L.sort.hist_off) +
+                             (size_t)(L.sort.passes - 1) * L.sort.bins;
+  const uint32_t* top_base = reinterpret_cast<const uint32_t*>(sort_ctrl + L.sort.base_off) +
+                             (size_t)(L.sort.passes - 1) * L.sort.bins;
+  if (msd) OCT_TRY(launch_msd_gate(top_hist, n, m.form, s), "build: sort form");
   uint32_t* sorted = keys_a;
-  OCT_TRY(launch_sort_passes(keys_a, keys_b, &L.sort, w + L.sort_off, m.status, s, &sorted, rec),
+  OCT_TRY(launch_sort_passes_split(keys_a, keys_b, &L.sort, sort_ctrl, m.status,
+                                   msd ? m.form + 1 : nullptr, s, &sorted, rec),
           "build: sort");
-  // Unique with the deltas of adjacent unique codes on the side; the tree
-  // (with the edge counts) comes from those deltas.
-  OCT_TRY(launch_unique_deltas(sorted, n, out->codes, m.unique, w + L.tree_off, s),
+  if (msd) {
+    OCT_TRY(launch_msd_scatter(keys_a, keys_b, &L.sort, sort_ctrl, m.status, m.form, s),
+            "build: msd scatter");
+  }
+  mark(rec, s);
+  if (msd) {
+    OCT_TRY(launch_msd_buckets(keys_b, top_base, top_hist, w + L.msd_off, m.form, m.status, s),
+            "build: msd buckets");
+  }
+  mark(rec, s);
+  OCT_TRY(launch_unique_deltas(sorted, n, out->codes, m.unique, w + L.tree_off, s,
+                               msd ? m.form + 1 : nullptr),
           "build: unique");
+  if (msd) {
+    OCT_TRY(launch_msd_pack(keys_b, top_base, n, out->codes, m.unique, w + L.msd_off,
+                            w + L.tree_off, m.form, s),
+            "build: msd pack");
+  }
   mark(rec, s);
   OCT_TRY(launch_radix_tree_from_deltas(n, m.unique, out->codes, out->tree.prefix_n,
                                         out->tree.has_leaf_left, out->tree.has_leaf_right,
@@ -422,9 +453,10 @@ int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range
 }
 
 static const char* const kBuildSteps[] = {
-    "start",        "clear",         "morton+histogram", "histogram scan", "sort pass 0",
-    "sort pass 1",  "sort pass 2",   "unique",           "radix tree+edge count", "prefix sum",
-    "octree emit",  "octree finalize",  "publish counts"};
+    "start",       "clear",       "morton+histogram", "histogram scan",
+    "sort pass 0", "sort pass 1", "sort pass 2",      "msd scatter",
+    "msd buckets", "unique",      "radix tree+edge count", "prefix sum",
+    "octree emit", "octree finalize", "publish counts"};
 
 int oct_build_step_count(void) { return (int)(sizeof(kBuildSteps) / sizeof(kBuildSteps[0])); }
 

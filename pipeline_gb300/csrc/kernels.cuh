@@ -85,6 +85,33 @@ cudaError_t launch_histogram_gated(const uint32_t* keys, const SortPlan* plan, v
 cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
                                      void* ctrl, uint32_t* status, const uint32_t* gate,
                                      cudaStream_t s, uint32_t** result);
+// The digit bases (exclusive scans of the Morton kernel's histograms), always
+// run; then the LSD passes gated on pass_gate (nullptr: always).
+cudaError_t launch_sort_passes_split(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
+                                     void* ctrl, uint32_t* status, const uint32_t* pass_gate,
+                                     cudaStream_t s, uint32_t** result, Recorder* rec);
+
+// ---- MSD form of stages 2-3 (whole builds of large, even clouds) ----------
+// The form is chosen on the device from the top-digit histogram: flags[0]
+// set runs the MSD kernels, flags[1] set the LSD passes and unique.
+int msd_min_n();
+size_t msd_scratch_bytes();
+bool msd_plan_ok(const SortPlan& p);  // 10-bit digits, 3 passes, reduce-then-scan
+cudaError_t launch_msd_gate(const uint32_t* top_hist, int n, uint32_t* flags, cudaStream_t s);
+// One unstable radix pass on the top digit (bits 20..29), keys -> out.
+cudaError_t launch_msd_scatter(const uint32_t* keys, uint32_t* out, const SortPlan* plan,
+                               void* ctrl, uint32_t* status, const uint32_t* gate,
+                               cudaStream_t s);
+// The sorted unique keys of every top-digit bucket over the front of its
+// range; the counts go to the scratch.
+cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const uint32_t* top_hist,
+                               void* scratch, const uint32_t* gate, uint32_t* status,
+                               cudaStream_t s);
+// Packs the bucket runs: codes, U to *d_unique, the adjacent deltas and tile
+// minima into the tree scratch (as launch_unique_deltas leaves them).
+cudaError_t launch_msd_pack(const uint32_t* keys, const uint32_t* top_base, int n,
+                            uint32_t* codes_out, int* d_unique, void* scratch,
+                            void* tree_scratch, const uint32_t* gate, cudaStream_t s);
 
 // ---- unique --------------------------------------------------------------
 struct ScanPlan {
@@ -129,7 +156,8 @@ TreeScratch tree_scratch_carve(void* base, int n_host);
 // but the first, the delta to the one before it into the tree scratch (and the
 // tiles' smallest deltas), so only tree_nodes_kernel remains of stage 4.
 cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_out, int* d_unique,
-                                 void* tree_scratch, cudaStream_t s);
+                                 void* tree_scratch, cudaStream_t s,
+                                 const uint32_t* gate = nullptr);
 // The same for batched clouds over their 4,096-key tiles (descriptors
 // {first, end, cloud, first tile of cloud}): each cloud's codes from its
 // start, its U to unique_c[cloud], its deltas in its own tree tiles.
@@ -148,7 +176,8 @@ cudaError_t launch_radix_tree_from_deltas(int n_host, const int* d_unique, const
                                           cudaStream_t s);
 // Exclusive scan of `tiles` counts into prefix (one CTA); total to *total_out.
 cudaError_t launch_tile_counts_scan(int tiles, const int* counts, uint32_t* prefix,
-                                    int* total_out, cudaStream_t s);
+                                    int* total_out, cudaStream_t s,
+                                    const uint32_t* gate = nullptr);
 size_t tree_scratch_bytes_tiles(int tiles);
 TreeScratch tree_scratch_carve_tiles(void* base, int tiles);
 // Batched clouds: tiles {first, end, cloud, first tile of cloud} of 4,096

@@ -366,7 +366,8 @@ constexpr int kTsThreads = 1024;
 __global__ void __launch_bounds__(kTsThreads)
     tile_sums_scan_kernel(int tiles_fixed, int n_host, const int* __restrict__ d_unique,
                           const int* __restrict__ tile_sum, uint32_t* __restrict__ tile_prefix,
-                          int* __restrict__ total_out) {
+                          int* __restrict__ total_out, const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
@@ -390,7 +391,7 @@ cudaError_t launch_prefix_sum_clear_tags(int n_host, const int* d_unique, int* e
   if (n_host <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve(tree_scratch, n_host);
   tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(0, n_host, d_unique, S.tile_sum, S.tile_prefix,
-                                                 nullptr);
+                                                 nullptr, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int tiles = (n_host + kEsTile - 1) / kEsTile;
@@ -426,14 +427,15 @@ cudaError_t launch_tile_sums_scan(int tiles, const int* tile_sum, uint32_t* tile
                                   cudaStream_t s) {
   if (tiles <= 0) return cudaSuccess;
   tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(tiles, 0, nullptr, tile_sum, tile_prefix,
-                                                 nullptr);
+                                                 nullptr, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tile_counts_scan(int tiles, const int* counts, uint32_t* prefix,
-                                    int* total_out, cudaStream_t s) {
+                                    int* total_out, cudaStream_t s, const uint32_t* gate) {
   if (tiles <= 0) return cudaSuccess;
-  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(tiles, 0, nullptr, counts, prefix, total_out);
+  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(tiles, 0, nullptr, counts, prefix, total_out,
+                                                 gate);
   return cudaGetLastError();
 }
 

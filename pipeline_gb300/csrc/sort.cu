@@ -631,7 +631,8 @@ cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* c
 
 static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
                                     void* ctrl, uint32_t* status, const uint32_t* gate,
-                                    cudaStream_t s, uint32_t** result, Recorder* rec) {
+                                    cudaStream_t s, uint32_t** result, Recorder* rec,
+                                    const uint32_t* pass_gate = nullptr) {
   *result = keys;
   if (plan->n <= 1) return cudaSuccess;
   char* c = static_cast<char*>(ctrl);
@@ -648,6 +649,7 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(rec, s);
+  if (pass_gate) gate = pass_gate;
   uint32_t* a = keys;
   uint32_t* b = alt;
   for (int p = 0; p < plan->passes; ++p) {
@@ -686,6 +688,36 @@ cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPl
                                      void* ctrl, uint32_t* status, const uint32_t* gate,
                                      cudaStream_t s, uint32_t** result) {
   return sort_passes_impl(keys, alt, plan, ctrl, status, gate, s, result, nullptr);
+}
+
+cudaError_t launch_sort_passes_split(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
+                                     void* ctrl, uint32_t* status, const uint32_t* pass_gate,
+                                     cudaStream_t s, uint32_t** result, Recorder* rec) {
+  return sort_passes_impl(keys, alt, plan, ctrl, status, nullptr, s, result, rec, pass_gate);
+}
+
+bool msd_plan_ok(const SortPlan& p) {
+  return p.radix_bits == 10 && p.passes == 3 && p.cfg.scan == 1;
+}
+
+cudaError_t launch_msd_scatter(const uint32_t* keys, uint32_t* out, const SortPlan* plan,
+                               void* ctrl, uint32_t* status, const uint32_t* gate,
+                               cudaStream_t s) {
+  if (plan->n <= 1 || !msd_plan_ok(*plan)) return cudaErrorInvalidValue;
+  char* c = static_cast<char*>(ctrl);
+  const int top = plan->passes - 1, bins = plan->bins, shift = top * plan->radix_bits;
+  const uint32_t* base = reinterpret_cast<uint32_t*>(c + plan->base_off) + (size_t)top * bins;
+  uint32_t* th = reinterpret_cast<uint32_t*>(c + plan->tile_hist_off);
+  // the top pass's split sums (the LSD top pass does not run in the same build)
+  uint32_t* pp = reinterpret_cast<uint32_t*>(c + plan->tile_part_off) + (size_t)top * kScanSplits * bins;
+  tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(keys, plan->n, shift, plan->tile, th, gate,
+                                                   nullptr, pp, plan->tiles);
+  tile_scan_split_kernel<<<dim3((bins + 31) / 32, kScanSplits), 1024, 0, s>>>(th, plan->tiles, bins,
+                                                                            base, pp, gate);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_pass(*plan, false, keys, out, shift, base, nullptr, nullptr, th, status, gate, s,
+                     nullptr, 0);
 }
 
 cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,

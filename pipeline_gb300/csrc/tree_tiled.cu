@@ -570,7 +570,9 @@ struct CloudKeys {
 // sums and smallest deltas.
 template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
-    unique_count_kernel(const uint32_t* __restrict__ keys, Map map, TreeScratch S) {
+    unique_count_kernel(const uint32_t* __restrict__ keys, Map map, TreeScratch S,
+                        const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ int s_cnt[kUdThreads / 32];
   const int t = blockIdx.x, tid = threadIdx.x;
   const KeyTile K = map(t);
@@ -626,7 +628,9 @@ __global__ void __launch_bounds__(kUdThreads)
 template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
     unique_deltas_kernel(const uint32_t* __restrict__ keys, Map map, uint32_t* __restrict__ out,
-                         TreeScratch S, int* __restrict__ unique_c) {
+                         TreeScratch S, int* __restrict__ unique_c,
+                         const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ uint32_t s_keys[kTtTile + kTtTile / 32];
   __shared__ uint8_t s_d[kTtTile];
   __shared__ uint32_t s_warp[32];
@@ -712,15 +716,16 @@ __global__ void __launch_bounds__(kUdThreads)
 }
 
 cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_out, int* d_unique,
-                                 void* tree_scratch, cudaStream_t s) {
+                                 void* tree_scratch, cudaStream_t s, const uint32_t* gate) {
   if (n <= 0) return cudaMemsetAsync(d_unique, 0, sizeof(int), s);
   const TreeScratch S = tree_scratch_carve(tree_scratch, n);
   const OneKeys map{n};
-  unique_count_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, S);
+  unique_count_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, S, gate);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = launch_tile_counts_scan(S.tiles, S.tile_heads, S.tile_upos, d_unique, s);
+  if (e == cudaSuccess)
+    e = launch_tile_counts_scan(S.tiles, S.tile_heads, S.tile_upos, d_unique, s, gate);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, nullptr);
+  unique_deltas_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, nullptr, gate);
   return cudaGetLastError();
 }
 
@@ -730,11 +735,11 @@ cudaError_t launch_batch_unique_deltas(const uint32_t* sorted, const int4* tiles
   if (n_tiles <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
   const CloudKeys map{tiles, n_tiles, start};
-  unique_count_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, S);
+  unique_count_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, S, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = launch_tile_counts_scan(n_tiles, S.tile_heads, S.tile_upos, nullptr, s);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, unique_c);
+  unique_deltas_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, unique_c, nullptr);
   return cudaGetLastError();
 }
 
