@@ -269,6 +269,16 @@ OCT_API int oct_build_octree(const oct_vec4* points, int n, float min_coord, flo
                      const oct_build_outputs* out, void* workspace, size_t workspace_bytes,
                      oct_stream_t stream);
 
+/* Which form stages 2-3 took in the last whole build of n points with this
+ * workspace (read back after that build has finished): 0 the LSD radix passes
+ * and run-head unique (clouds below 2^22 points), 1 the MSD form (top-digit
+ * scatter, per-bucket bitmaps, pack), 2 the LSD form chosen by the device
+ * because the top-digit buckets were too uneven. Both give the same bytes. */
+#define OCT_SORT_FORM_LSD 0
+#define OCT_SORT_FORM_MSD 1
+#define OCT_SORT_FORM_LSD_FALLBACK 2
+OCT_API int oct_build_sort_form(const void* workspace, int n, int nodes_capacity, int* form);
+
 /* Timed build for measurement: the same launches as oct_build_octree, with
  * caller-created CUDA events (cudaEvent_t, passed as void*) recorded on the
  * stream at each step boundary: events[k] after step k of

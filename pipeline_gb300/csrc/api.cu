@@ -458,6 +458,22 @@ static const char* const kBuildSteps[] = {
     "msd buckets", "unique",      "radix tree+edge count", "prefix sum",
     "octree emit", "octree finalize", "publish counts"};
 
+int oct_build_sort_form(const void* workspace, int n, int nodes_capacity, int* form) {
+  if (!workspace || !form || n < 0 || n > OCT_MAX_N || nodes_capacity < 0)
+    return OCT_ERR_INVALID_ARG;
+  const BuildLayout L = build_layout(n, nodes_capacity);
+  if (n < msd_min_n() || !msd_plan_ok(L.sort)) {
+    *form = OCT_SORT_FORM_LSD;
+    return OCT_OK;
+  }
+  uint32_t f[2] = {0, 0};
+  OCT_TRY(cudaMemcpy(f, static_cast<const char*>(workspace) + L.misc_off + 16, sizeof(f),
+                     cudaMemcpyDeviceToHost),
+          "oct_build_sort_form");
+  *form = f[0] ? OCT_SORT_FORM_MSD : OCT_SORT_FORM_LSD_FALLBACK;
+  return OCT_OK;
+}
+
 int oct_build_step_count(void) { return (int)(sizeof(kBuildSteps) / sizeof(kBuildSteps[0])); }
 
 const char* oct_build_step_name(int k) {

@@ -84,6 +84,17 @@ class OctreeBuilder:
                                        C.byref(self._out), C.c_void_p(self.workspace.data_ptr()),
                                        self.workspace.numel(), C.c_void_p(s.cuda_stream))
         _lib.check(rc, "oct_build_octree")
+        self._last_n = n
+
+    def sort_form(self) -> int:
+        """Form of stages 2-3 in the last build (synchronises): 0 LSD passes,
+        1 MSD form, 2 LSD chosen by the device for an uneven cloud."""
+        torch.cuda.synchronize(self.device)
+        f = C.c_int(-1)
+        _lib.check(self.lib.oct_build_sort_form(C.c_void_p(self.workspace.data_ptr()),
+                                                getattr(self, "_last_n", self.n_max), self.cap,
+                                                C.byref(f)), "oct_build_sort_form")
+        return f.value
 
     def counts(self) -> BuildCounts:
         """Synchronise and read {U, U-1, M, status}."""

@@ -1,0 +1,64 @@
+"""GPU parity of the whole build's two forms of stages 2-3 on clouds large
+enough (2^22+ points) for the MSD form to be considered: the device takes the
+MSD form (top-digit scatter, per-bucket bitmaps, pack) for even clouds and
+falls back to the LSD radix passes for uneven ones; both must give the
+oracle's bytes for every stage output."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+STAGES = ["sorted_unique", "prefix_n", "has_leaf_left", "has_leaf_right", "left_child", "parent",
+          "edge_count", "prefix_sum", "oct_nodes"]
+MIN_N = 1 << 22
+
+
+def _build(pts):
+    from pipeline_gb300.pipeline import OctreeBuilder
+
+    n = len(pts)
+    b = OctreeBuilder(n)
+    b.build(torch.from_numpy(np.ascontiguousarray(pts)).cuda(), 0.0, 1024.0)
+    return b.result(), b.sort_form()
+
+
+def _check(pts, form, label):
+    res, got_form = _build(pts)
+    assert got_form == form, (label, got_form)
+    expect = O.build_all(pts, 0.0, 1024.0)
+    assert (res["n_unique"], res["n_oct"], res["status"]) == \
+        (expect["n_unique"], expect["n_oct"], 0), label
+    for key in STAGES:
+        assert res[key].tobytes() == np.asarray(expect[key]).tobytes(), (label, key)
+
+
+def test_msd_form_even_cloud_with_duplicates():
+    # points on a 1/4-unit grid: many cells hold several points (duplicate codes)
+    rng = np.random.default_rng(5)
+    n = MIN_N + 12345
+    pts = np.ones((n, 4), np.float32)
+    pts[:, :3] = np.floor(rng.uniform(0, 1024, (n, 3)) * 4) / 4
+    _check(pts, 1, "grid")
+
+
+def test_msd_form_even_cloud():
+    n = MIN_N + 1
+    _check(O.init_random_vec4(n, 0.0, 1024.0, seed=77), 1, "uniform")
+
+
+def test_lsd_fallback_for_uneven_cloud():
+    rng = np.random.default_rng(9)
+    n = MIN_N + 777
+    c = rng.uniform(100, 900, (6, 3))
+    idx = rng.integers(0, 6, n)
+    pts = np.ones((n, 4), np.float32)
+    pts[:, :3] = np.clip(rng.normal(c[idx], 12.0), 0, np.nextafter(np.float32(1024), 0))
+    _check(pts, 2, "clusters")
+
+
+def test_below_msd_size_uses_lsd():
+    n = MIN_N - 1
+    _check(O.init_random_vec4(n, 0.0, 1024.0, seed=3), 0, "below")
