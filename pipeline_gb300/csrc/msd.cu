@@ -29,6 +29,7 @@ constexpr int kMsdSpanBits = 20;                       // key bits below the top
 constexpr int kMsdBuckets = 1 << (30 - kMsdSpanBits);  // 1,024
 constexpr int kMsdWords = 1 << (kMsdSpanBits - 5);     // bitmap words per bucket
 constexpr int kMsdThreads = 1024;
+constexpr int kMsdStage = 24576;  // run keys staged in shared memory behind the bitmap
 constexpr int kMsdWarpWords = kMsdWords / (kMsdThreads / 32);
 constexpr int kMsdMinN = 1 << 22;
 constexpr uint32_t kMsdSkew = 4;
@@ -107,9 +108,12 @@ __global__ void __launch_bounds__(kMsdThreads, 1)
     wd[4 * j + 2] = v.z;
     wd[4 * j + 3] = v.w;
   }
-  uint32_t own = 0;
+  uint32_t own = 0, nz = 0;  // set bits, and the words that have any
 #pragma unroll
-  for (int k = 0; k < 32; ++k) own += __popc(wd[k]);
+  for (int k = 0; k < 32; ++k) {
+    own += __popc(wd[k]);
+    nz |= (wd[k] != 0u ? 1u : 0u) << k;
+  }
   uint32_t inc = own;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -117,7 +121,7 @@ __global__ void __launch_bounds__(kMsdThreads, 1)
     if (lane >= o) inc += t;
   }
   if (lane == 31) s_wsum[w] = inc;
-  __syncthreads();  // every word is in registers: the bitmap becomes the output stage
+  __syncthreads();
   uint32_t pos = inc - own, total = 0;
 #pragma unroll 8
   for (int k = 0; k < kMsdThreads / 32; ++k) {
@@ -127,25 +131,31 @@ __global__ void __launch_bounds__(kMsdThreads, 1)
   }
   if (tid == 0) ucount[b] = total;
   // Every key was read before the first barrier: the run overwrites the front
-  // of the bucket's own range, staged in the bitmap's storage when it fits
-  // there (kMsdWords keys), else written straight out. `total` is the same in
-  // every thread, so the branch is uniform.
+  // of the bucket's own range, staged behind the bitmap when it fits there
+  // (kMsdStage keys), else written straight out. `total` is the same in
+  // every thread, so the branch is uniform. A lane walks its own set bits in
+  // one loop (words re-read from the bitmap), so a warp runs as many rounds
+  // as its fullest lane has keys.
   uint32_t* out = keys + lo;
-  const bool staged = total <= (uint32_t)kMsdWords;
-  uint32_t* dst = staged ? bm : out;
+  uint32_t* stage = bm + kMsdWords;
+  const bool staged = total <= (uint32_t)kMsdStage;
+  uint32_t* dst = staged ? stage : out;
   const uint32_t kc = ((uint32_t)b << kMsdSpanBits) | ((uint32_t)c << 10);
-#pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    uint32_t bits = wd[k];
-    while (bits) {
-      const int bit = __ffs(bits) - 1;
-      bits &= bits - 1u;
-      dst[pos++] = kc | ((uint32_t)k << 5) | (uint32_t)bit;
+  uint32_t bits = 0, kw = 0;
+  for (uint32_t e = 0; e < own; ++e) {
+    if (bits == 0u) {
+      const int k = __ffs(nz) - 1;
+      nz &= nz - 1u;
+      kw = kc | ((uint32_t)k << 5);
+      bits = bm[msd_swz((uint32_t)(c * 32 + k))];
     }
+    const int bit = __ffs(bits) - 1;
+    bits &= bits - 1u;
+    dst[pos + e] = kw | (uint32_t)bit;
   }
   if (staged) {
     __syncthreads();
-    for (uint32_t i = tid; i < total; i += kMsdThreads) out[i] = bm[i];
+    for (uint32_t i = tid; i < total; i += kMsdThreads) out[i] = stage[i];
   }
 }
 
@@ -268,7 +278,7 @@ cudaError_t launch_msd_gate(const uint32_t* top_hist, int n, uint32_t* flags, cu
 cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const uint32_t* top_hist,
                                void* scratch, const uint32_t* gate, uint32_t* status,
                                cudaStream_t s) {
-  constexpr int smem = sizeof(uint32_t) * kMsdWords;
+  constexpr int smem = sizeof(uint32_t) * (kMsdWords + kMsdStage);
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(msd_bucket_kernel,
