@@ -56,8 +56,8 @@ WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 
 # as fixed by the octree-build analysis: stage 1 reads 16 B and writes 4 B per
 # point (its digit histograms are fused, so the sort reads no extra 4 B/key);
 # each 10-bit sort pass reads and writes 4 B per key; unique reads 4 B per key
-# and writes 4 B per unique key (in the MSD form of large even clouds: one
-# scatter pass of 8 B per key, the bucket bitmaps reading 4 B per key and
+# and writes 4 B per unique key (in the MSD form of large even clouds: pass 0
+# scatters on the top digit, 8 B per key, the bucket bitmaps reading 4 B per key and
 # writing 4 B per unique key, and the pack reading 4 B and writing 5 B per
 # unique key: code and delta); the radix tree with its edge counts reads 4 B
 # per code and writes 15 B per node (11 B of tree + 4 B of edge count); the
@@ -65,8 +65,8 @@ WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 
 # leaf link (split over the emit and finalize launches).
 def algorithmic_bytes(n, u, b, m, msd=False):
     leaves = b + 1
-    if msd:  # MSD form: one scatter pass, bucket bitmaps, pack (codes + deltas)
-        sort = {"msd scatter": 8 * n, "msd buckets": 4 * n + 4 * u, "unique": 9 * u}
+    if msd:  # MSD form: pass 0's launches scatter on the top digit, bucket bitmaps, pack
+        sort = {"sort pass 0": 8 * n, "msd buckets": 4 * n + 4 * u, "unique": 9 * u}
     else:
         sort = {"sort pass 0": 8 * n, "sort pass 1": 8 * n, "sort pass 2": 8 * n,
                 "unique": 4 * n + 4 * u}
@@ -472,9 +472,10 @@ def build_launches(n: int = 0) -> int:
     rb, _, _, scan = autotune.get_config()
     passes = (30 + rb - 1) // rb
     lsd = 2 + passes * (3 if scan == 1 else 1) + 3 + 1 + 2 + 2 + 1
-    # MSD form (launched beside the LSD passes for clouds of 2^22+ points):
-    # form gate, top-digit scatter (3), bucket bitmaps, pack scan + pack
-    msd = 7 if (n >= (1 << 22) and rb == 10 and passes == 3 and scan == 1) else 0
+    # MSD form (launched beside the LSD passes for clouds of 2^22+ points; pass
+    # 0's launches double as its top-digit scatter): form gate, bucket
+    # bitmaps, pack scan + pack
+    msd = 4 if (n >= (1 << 22) and rb == 10 and passes == 3 and scan == 1) else 0
     return lsd + msd
 
 

@@ -385,13 +385,9 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
   if (msd) OCT_TRY(launch_msd_gate(top_hist, n, m.form, s), "build: sort form");
   uint32_t* sorted = keys_a;
   OCT_TRY(launch_sort_passes_split(keys_a, keys_b, &L.sort, sort_ctrl, m.status,
-                                   msd ? m.form + 1 : nullptr, s, &sorted, rec),
+                                   msd ? m.form : nullptr, msd ? m.form + 1 : nullptr, s, &sorted,
+                                   rec),
           "build: sort");
-  if (msd) {
-    OCT_TRY(launch_msd_scatter(keys_a, keys_b, &L.sort, sort_ctrl, m.status, m.form, s),
-            "build: msd scatter");
-  }
-  mark(rec, s);
   if (msd) {
     OCT_TRY(launch_msd_buckets(keys_b, top_base, top_hist, w + L.msd_off, m.form, m.status, s),
             "build: msd buckets");
@@ -454,9 +450,9 @@ int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range
 
 static const char* const kBuildSteps[] = {
     "start",       "clear",       "morton+histogram", "histogram scan",
-    "sort pass 0", "sort pass 1", "sort pass 2",      "msd scatter",
-    "msd buckets", "unique",      "radix tree+edge count", "prefix sum",
-    "octree emit", "octree finalize", "publish counts"};
+    "sort pass 0", "sort pass 1", "sort pass 2",      "msd buckets",
+    "unique",      "radix tree+edge count", "prefix sum", "octree emit",
+    "octree finalize", "publish counts"};
 
 int oct_build_sort_form(const void* workspace, int n, int nodes_capacity, int* form) {
   if (!workspace || !form || n < 0 || n > OCT_MAX_N || nodes_capacity < 0)

@@ -60,10 +60,19 @@ SortPlan sort_plan(int n, int key_bits);
 SortPlan sort_plan_cfg(int n, int key_bits, SortConfig cfg);
 // One digit pass (batched sorts: tile descriptors int4{first, end, cloud,
 // first tile of cloud} and their count; nullptr / 0 for a single array).
+// A launch that serves as either of two passes, chosen on the device: when
+// *flag != 0 the tile histogram, tile scan and pass kernels use this shift,
+// these digit bases and these split sums instead of their own.
+struct DigitAlt {
+  const uint32_t* flag = nullptr;
+  int shift = 0;
+  const uint32_t* base = nullptr;
+  uint32_t* part = nullptr;
+};
 cudaError_t launch_pass(const SortPlan& p, bool stable, const uint32_t* src, uint32_t* dst,
                         int shift, const uint32_t* base, uint32_t* lookback, uint32_t* counter,
                         const uint32_t* tile_prefix, uint32_t* status, const uint32_t* gate,
-                        cudaStream_t s, const int4* tdesc, int tiles);
+                        cudaStream_t s, const int4* tdesc, int tiles, DigitAlt alt = DigitAlt{});
 cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
                              const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s);
 void set_sort_config(const SortConfig& c);
@@ -86,10 +95,13 @@ cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPl
                                      void* ctrl, uint32_t* status, const uint32_t* gate,
                                      cudaStream_t s, uint32_t** result);
 // The digit bases (exclusive scans of the Morton kernel's histograms), always
-// run; then the LSD passes gated on pass_gate (nullptr: always).
+// run; then the LSD passes. With msd_flag (device): pass 0's launches do the
+// MSD form's top-digit scatter instead when *msd_flag != 0, and passes 1..
+// are gated on lsd_flag.
 cudaError_t launch_sort_passes_split(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
-                                     void* ctrl, uint32_t* status, const uint32_t* pass_gate,
-                                     cudaStream_t s, uint32_t** result, Recorder* rec);
+                                     void* ctrl, uint32_t* status, const uint32_t* msd_flag,
+                                     const uint32_t* lsd_flag, cudaStream_t s, uint32_t** result,
+                                     Recorder* rec);
 
 // ---- MSD form of stages 2-3 (whole builds of large, even clouds) ----------
 // The form is chosen on the device from the top-digit histogram: flags[0]
@@ -98,10 +110,6 @@ int msd_min_n();
 size_t msd_scratch_bytes();
 bool msd_plan_ok(const SortPlan& p);  // 10-bit digits, 3 passes, reduce-then-scan
 cudaError_t launch_msd_gate(const uint32_t* top_hist, int n, uint32_t* flags, cudaStream_t s);
-// One unstable radix pass on the top digit (bits 20..29), keys -> out.
-cudaError_t launch_msd_scatter(const uint32_t* keys, uint32_t* out, const SortPlan* plan,
-                               void* ctrl, uint32_t* status, const uint32_t* gate,
-                               cudaStream_t s);
 // The sorted unique keys of every top-digit bucket over the front of its
 // range; the counts go to the scratch.
 cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const uint32_t* top_hist,

@@ -8,10 +8,11 @@
 //            than 4x the mean; otherwise the LSD passes and the run-head
 //            unique run. Both forms are launched; the unused one's kernels
 //            return at once (a device flag each).
-//   scatter  one unstable radix pass on the top digit (the LSD pass kernel
-//            with the top digit's bases), so bucket b holds the keys
+//   scatter  one unstable radix pass on the top digit: the LSD form's pass-0
+//            launches, which take the top digit's shift, bases and split sums
+//            when the MSD flag is set, so bucket b holds the keys
 //            [b << 20, (b + 1) << 20) in any order;
-//   buckets  one CTA per bucket: a 2^20-bit bitmap (128 KiB of shared memory)
+//   buckets  one CTA per SM walks the buckets: a 2^20-bit bitmap (128 KiB of shared memory)
 //            marks the bucket's keys; its set bits, read in order, are the
 //            bucket's sorted unique keys (duplicates mark the same bit),
 //            written over the front of the bucket's own range;
@@ -20,6 +21,8 @@
 //            next (the radix tree's input) and lowers the minima of the tree
 //            tiles it touches: the same outputs as the LSD form's unique
 //            stage.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "tree.cuh"
 
@@ -62,16 +65,12 @@ __global__ void __launch_bounds__(kMsdBuckets)
 // load phase read eight different bank groups.
 __device__ __forceinline__ uint32_t msd_swz(uint32_t x) { return x ^ (((x >> 5) & 7u) << 2); }
 
-__global__ void __launch_bounds__(kMsdThreads, 1)
-    msd_bucket_kernel(uint32_t* __restrict__ keys, const uint32_t* __restrict__ top_base,
-                      const uint32_t* __restrict__ top_hist, uint32_t* __restrict__ ucount,
-                      const uint32_t* __restrict__ gate, uint32_t* __restrict__ status) {
-  if (*gate == 0) return;
-  extern __shared__ uint4 s_bm4[];
-  uint32_t* bm = reinterpret_cast<uint32_t*>(s_bm4);
-  __shared__ uint32_t s_wsum[kMsdThreads / 32];
-  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const uint32_t lo = top_base[b], cnt = top_hist[b];
+__device__ __forceinline__ void msd_bucket(uint32_t* __restrict__ keys, uint32_t lo, uint32_t cnt,
+                                           int b, uint32_t* bm, uint32_t* s_wsum,
+                                           uint32_t* __restrict__ ucount,
+                                           uint32_t* __restrict__ status, int tid, int lane,
+                                           int w) {
+  uint4* s_bm4 = reinterpret_cast<uint4*>(bm);
   for (int i = tid; i < kMsdWords / 4; i += kMsdThreads) s_bm4[i] = make_uint4(0u, 0u, 0u, 0u);
   __syncthreads();
   bool bad = false;
@@ -159,6 +158,22 @@ __global__ void __launch_bounds__(kMsdThreads, 1)
   }
 }
 
+__global__ void __launch_bounds__(kMsdThreads, 1)
+    msd_bucket_kernel(uint32_t* __restrict__ keys, const uint32_t* __restrict__ top_base,
+                      const uint32_t* __restrict__ top_hist, uint32_t* __restrict__ ucount,
+                      const uint32_t* __restrict__ gate, uint32_t* __restrict__ status) {
+  if (*gate == 0) return;
+  extern __shared__ uint4 s_bm4[];
+  uint32_t* bm = reinterpret_cast<uint32_t*>(s_bm4);
+  __shared__ uint32_t s_wsum[kMsdThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  // one CTA per SM (its shared memory) walks the buckets
+  for (int b = blockIdx.x; b < kMsdBuckets; b += gridDim.x) {
+    msd_bucket(keys, top_base[b], top_hist[b], b, bm, s_wsum, ucount, status, tid, lane, w);
+    __syncthreads();  // the next bucket clears the bitmap and the stage
+  }
+}
+
 __global__ void __launch_bounds__(kMsdBuckets)
     msd_pack_scan_kernel(const uint32_t* __restrict__ ucount, uint32_t* __restrict__ uoff,
                          int* __restrict__ next_start, const uint32_t* __restrict__ top_base,
@@ -197,22 +212,11 @@ __global__ void __launch_bounds__(kMsdBuckets)
 
 constexpr int kPackTiles = 1028;  // tree tiles one bucket's run can touch (4x the mean of 2^20)
 
-// One CTA per bucket: its run goes to the codes from the run's output offset,
-// with each code's delta to the next one (the next bucket's first code after
-// the run's last) and the touched tree tiles' minima.
-__global__ void __launch_bounds__(kPackThreads)
-    msd_pack_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ top_base,
-                    const uint32_t* __restrict__ ucount, const uint32_t* __restrict__ uoff,
-                    const int* __restrict__ next_start, uint32_t* __restrict__ codes,
-                    TreeScratch S, const uint32_t* __restrict__ gate) {
-  if (*gate == 0) return;
-  __shared__ uint32_t s_tmin[kPackTiles];
-  const int b = blockIdx.x, tid = threadIdx.x;
-  const uint32_t u = ucount[b];
-  if (u == 0) return;
-  const uint32_t U = uoff[kMsdBuckets], o0 = uoff[b];
-  const uint32_t* src = keys + top_base[b];
-  const int ns = next_start[b];
+__device__ __forceinline__ void msd_pack_run(const uint32_t* __restrict__ keys, uint32_t start,
+                                             uint32_t u, uint32_t o0, uint32_t U, int ns,
+                                             uint32_t* __restrict__ codes, const TreeScratch& S,
+                                             uint32_t* s_tmin, int tid) {
+  const uint32_t* src = keys + start;
   const uint32_t after = ns >= 0 ? keys[ns] : 0u;  // read only when a code follows the run
   const uint32_t t0 = o0 / kTtTile;
   const uint32_t nt = min((o0 + u - 1) / kTtTile - t0 + 1, (uint32_t)kPackTiles);
@@ -270,6 +274,25 @@ __global__ void __launch_bounds__(kPackThreads)
     if (s_tmin[k] < kTtAbsent) atomic_min_u8(S.tile_min + t0 + k, s_tmin[k]);
 }
 
+// CTAs walk the buckets: a run goes to the codes from its output offset, with
+// each code's delta to the next one (the next bucket's first code after the
+// run's last) and the touched tree tiles' minima.
+__global__ void __launch_bounds__(kPackThreads)
+    msd_pack_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ top_base,
+                    const uint32_t* __restrict__ ucount, const uint32_t* __restrict__ uoff,
+                    const int* __restrict__ next_start, uint32_t* __restrict__ codes,
+                    TreeScratch S, const uint32_t* __restrict__ gate) {
+  if (*gate == 0) return;
+  __shared__ uint32_t s_tmin[kPackTiles];
+  const int tid = threadIdx.x;
+  for (int b = blockIdx.x; b < kMsdBuckets; b += gridDim.x) {
+    const uint32_t u = ucount[b];
+    if (u != 0) msd_pack_run(keys, top_base[b], u, uoff[b], uoff[kMsdBuckets], next_start[b],
+                             codes, S, s_tmin, tid);
+    __syncthreads();  // s_tmin is the next run's
+  }
+}
+
 cudaError_t launch_msd_gate(const uint32_t* top_hist, int n, uint32_t* flags, cudaStream_t s) {
   msd_gate_kernel<<<1, kMsdBuckets, 0, s>>>(top_hist, n, flags);
   return cudaGetLastError();
@@ -287,7 +310,8 @@ cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const u
     attr = true;
   }
   uint32_t* ucount = static_cast<uint32_t*>(scratch);
-  msd_bucket_kernel<<<kMsdBuckets, kMsdThreads, smem, s>>>(keys, top_base, top_hist, ucount, gate,
+  const int grid = std::min(kMsdBuckets, device_sm_count());  // one CTA fits an SM
+  msd_bucket_kernel<<<grid, kMsdThreads, smem, s>>>(keys, top_base, top_hist, ucount, gate,
                                                            status);
   return cudaGetLastError();
 }

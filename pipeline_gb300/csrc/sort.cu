@@ -175,8 +175,13 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
                      int shift, const uint32_t* __restrict__ bin_base,
                      uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter,
                      const uint32_t* __restrict__ tile_prefix, uint32_t* __restrict__ status,
-                     const uint32_t* __restrict__ gate, const int4* __restrict__ tdesc) {
+                     const uint32_t* __restrict__ gate, const int4* __restrict__ tdesc,
+                     DigitAlt alt) {
   if (gate && *gate == 0) return;
+  if (alt.flag && *alt.flag) {
+    shift = alt.shift;
+    bin_base = alt.base;
+  }
   using L = PassSmem<RB, WARPS, ITEMS, STABLE>;
   constexpr int BINS = L::BINS, THREADS = WARPS * 32, TILE = L::TILE;
   constexpr uint32_t MASK = BINS - 1;
@@ -410,8 +415,13 @@ template <int RB>
 __global__ void __launch_bounds__(256)
     tile_hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tile_keys,
                      uint32_t* __restrict__ th, const uint32_t* __restrict__ gate,
-                     const int4* __restrict__ tdesc, uint32_t* __restrict__ part, int tiles) {
+                     const int4* __restrict__ tdesc, uint32_t* __restrict__ part, int tiles,
+                     DigitAlt alt) {
   if (gate && *gate == 0) return;
+  if (alt.flag && *alt.flag) {
+    shift = alt.shift;
+    part = alt.part;
+  }
   constexpr int BINS = 1 << RB;
   __shared__ uint32_t h[BINS];
   for (int b = threadIdx.x; b < BINS; b += 256) h[b] = 0;
@@ -448,8 +458,12 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(1024)
     tile_scan_split_kernel(uint32_t* __restrict__ th, int tiles, int bins,
                            const uint32_t* __restrict__ bin_base, const uint32_t* __restrict__ part,
-                           const uint32_t* __restrict__ gate) {
+                           const uint32_t* __restrict__ gate, DigitAlt alt) {
   if (gate && *gate == 0) return;
+  if (alt.flag && *alt.flag) {
+    bin_base = alt.base;
+    part = alt.part;
+  }
   __shared__ uint32_t sums[32][33];
   const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + l;
@@ -536,7 +550,7 @@ static cudaError_t launch_pass_t(const uint32_t* src, uint32_t* dst, int n, int 
                                  const uint32_t* base, uint32_t* lookback, uint32_t* counter,
                                  const uint32_t* tile_prefix, uint32_t* status,
                                  const uint32_t* gate, cudaStream_t s, const int4* tdesc,
-                                 int tiles_override) {
+                                 int tiles_override, DigitAlt alt) {
   using L = PassSmem<RB, WARPS, ITEMS, STABLE>;
   auto k = sort_pass_kernel<RB, WARPS, ITEMS, STABLE, SCAN>;
   static bool attr = false;
@@ -546,7 +560,7 @@ static cudaError_t launch_pass_t(const uint32_t* src, uint32_t* dst, int n, int 
   }
   const int tiles = tiles_override > 0 ? tiles_override : (n + L::TILE - 1) / L::TILE;
   k<<<tiles, WARPS * 32, L::BYTES, s>>>(src, dst, n, shift, base, lookback, counter, tile_prefix,
-                                        status, gate, tdesc);
+                                        status, gate, tdesc, alt);
   return cudaGetLastError();
 }
 
@@ -555,35 +569,35 @@ static cudaError_t launch_pass_cfg(bool stable, int scan, const uint32_t* src, u
                                    int n, int shift, const uint32_t* base, uint32_t* lookback,
                                    uint32_t* counter, const uint32_t* tile_prefix,
                                    uint32_t* status, const uint32_t* gate, cudaStream_t s,
-                                   const int4* tdesc, int tiles) {
+                                   const int4* tdesc, int tiles, DigitAlt alt) {
   if (stable)
     return scan == 0 ? launch_pass_t<RB, WARPS, ITEMS, true, 0>(src, dst, n, shift, base, lookback,
-                                                                 counter, tile_prefix, status, gate, s, tdesc, tiles)
+                                                                 counter, tile_prefix, status, gate, s, tdesc, tiles, alt)
                      : launch_pass_t<RB, WARPS, ITEMS, true, 1>(src, dst, n, shift, base, lookback,
-                                                                 counter, tile_prefix, status, gate, s, tdesc, tiles);
+                                                                 counter, tile_prefix, status, gate, s, tdesc, tiles, alt);
   return scan == 0 ? launch_pass_t<RB, WARPS, ITEMS, false, 0>(src, dst, n, shift, base, lookback,
-                                                                counter, tile_prefix, status, gate, s, tdesc, tiles)
+                                                                counter, tile_prefix, status, gate, s, tdesc, tiles, alt)
                    : launch_pass_t<RB, WARPS, ITEMS, false, 1>(src, dst, n, shift, base, lookback,
-                                                                counter, tile_prefix, status, gate, s, tdesc, tiles);
+                                                                counter, tile_prefix, status, gate, s, tdesc, tiles, alt);
 }
 
 cudaError_t launch_pass(const SortPlan& p, bool stable, const uint32_t* src, uint32_t* dst,
                         int shift, const uint32_t* base, uint32_t* lookback, uint32_t* counter,
                         const uint32_t* tile_prefix, uint32_t* status, const uint32_t* gate,
-                        cudaStream_t s, const int4* tdesc, int tiles) {
+                        cudaStream_t s, const int4* tdesc, int tiles, DigitAlt alt) {
   const int sc = p.cfg.scan;
   if (p.radix_bits == 10) {
     if (p.cfg.items == 24)
       return launch_pass_cfg<10, 16, 24>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
-                                         tile_prefix, status, gate, s, tdesc, tiles);
+                                         tile_prefix, status, gate, s, tdesc, tiles, alt);
     return launch_pass_cfg<10, 16, 16>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
-                                       tile_prefix, status, gate, s, tdesc, tiles);
+                                       tile_prefix, status, gate, s, tdesc, tiles, alt);
   }
   if (p.cfg.items == 24)
     return launch_pass_cfg<8, 16, 24>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
-                                      tile_prefix, status, gate, s, tdesc, tiles);
+                                      tile_prefix, status, gate, s, tdesc, tiles, alt);
   return launch_pass_cfg<8, 16, 16>(stable, sc, src, dst, p.n, shift, base, lookback, counter,
-                                    tile_prefix, status, gate, s, tdesc, tiles);
+                                    tile_prefix, status, gate, s, tdesc, tiles, alt);
 }
 
 cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float min_coord,
@@ -632,7 +646,8 @@ cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* c
 static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
                                     void* ctrl, uint32_t* status, const uint32_t* gate,
                                     cudaStream_t s, uint32_t** result, Recorder* rec,
-                                    const uint32_t* pass_gate = nullptr) {
+                                    const uint32_t* msd_flag = nullptr,
+                                    const uint32_t* lsd_flag = nullptr) {
   *result = keys;
   if (plan->n <= 1) return cudaSuccess;
   char* c = static_cast<char*>(ctrl);
@@ -649,25 +664,38 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(rec, s);
-  if (pass_gate) gate = pass_gate;
+  // The MSD form's top-digit scatter reuses pass 0's launches (unstable, the
+  // top digit's shift, bases and split sums, chosen on the device); the later
+  // passes then return at once.
+  DigitAlt alt0;
+  if (msd_flag && msd_plan_ok(*plan)) {
+    const int top = plan->passes - 1;
+    alt0.flag = msd_flag;
+    alt0.shift = top * plan->radix_bits;
+    alt0.base = base + (size_t)top * plan->bins;
+    alt0.part = part + (size_t)top * kScanSplits * plan->bins;
+  }
   uint32_t* a = keys;
   uint32_t* b = alt;
   for (int p = 0; p < plan->passes; ++p) {
     const int shift = p * plan->radix_bits;
+    const uint32_t* g = (p > 0 && lsd_flag) ? lsd_flag : gate;
+    const DigitAlt da = p == 0 ? alt0 : DigitAlt{};
     if (plan->cfg.scan == 1) {
       uint32_t* pp = part + (size_t)p * kScanSplits * plan->bins;
       if (plan->radix_bits == 10)
-        tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gate,
-                                                         nullptr, pp, plan->tiles);
+        tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
+                                                         nullptr, pp, plan->tiles, da);
       else
-        tile_hist_kernel<8><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gate,
-                                                        nullptr, pp, plan->tiles);
+        tile_hist_kernel<8><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
+                                                        nullptr, pp, plan->tiles, da);
       tile_scan_split_kernel<<<dim3((plan->bins + 31) / 32, kScanSplits), 1024, 0, s>>>(
-          th, plan->tiles, plan->bins, base + p * plan->bins, pp, gate);
+          th, plan->tiles, plan->bins, base + p * plan->bins, pp, g, da);
     }
     uint32_t* lb = lookback + (size_t)p * plan->tiles * plan->bins;
     e = launch_pass(*plan, p > 0, a, b, shift, base + p * plan->bins,
-                    plan->cfg.scan == 0 ? lb : nullptr, counters + p, th, status, gate, s, nullptr, 0);
+                    plan->cfg.scan == 0 ? lb : nullptr, counters + p, th, status, g, s, nullptr, 0,
+                    da);
     if (e != cudaSuccess) return e;
     mark(rec, s);
     uint32_t* t = a;
@@ -691,43 +719,25 @@ cudaError_t launch_sort_passes_gated(uint32_t* keys, uint32_t* alt, const SortPl
 }
 
 cudaError_t launch_sort_passes_split(uint32_t* keys, uint32_t* alt, const SortPlan* plan,
-                                     void* ctrl, uint32_t* status, const uint32_t* pass_gate,
-                                     cudaStream_t s, uint32_t** result, Recorder* rec) {
-  return sort_passes_impl(keys, alt, plan, ctrl, status, nullptr, s, result, rec, pass_gate);
+                                     void* ctrl, uint32_t* status, const uint32_t* msd_flag,
+                                     const uint32_t* lsd_flag, cudaStream_t s, uint32_t** result,
+                                     Recorder* rec) {
+  return sort_passes_impl(keys, alt, plan, ctrl, status, nullptr, s, result, rec, msd_flag,
+                          lsd_flag);
 }
 
 bool msd_plan_ok(const SortPlan& p) {
   return p.radix_bits == 10 && p.passes == 3 && p.cfg.scan == 1;
 }
 
-cudaError_t launch_msd_scatter(const uint32_t* keys, uint32_t* out, const SortPlan* plan,
-                               void* ctrl, uint32_t* status, const uint32_t* gate,
-                               cudaStream_t s) {
-  if (plan->n <= 1 || !msd_plan_ok(*plan)) return cudaErrorInvalidValue;
-  char* c = static_cast<char*>(ctrl);
-  const int top = plan->passes - 1, bins = plan->bins, shift = top * plan->radix_bits;
-  const uint32_t* base = reinterpret_cast<uint32_t*>(c + plan->base_off) + (size_t)top * bins;
-  uint32_t* th = reinterpret_cast<uint32_t*>(c + plan->tile_hist_off);
-  // the top pass's split sums (the LSD top pass does not run in the same build)
-  uint32_t* pp = reinterpret_cast<uint32_t*>(c + plan->tile_part_off) + (size_t)top * kScanSplits * bins;
-  tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(keys, plan->n, shift, plan->tile, th, gate,
-                                                   nullptr, pp, plan->tiles);
-  tile_scan_split_kernel<<<dim3((bins + 31) / 32, kScanSplits), 1024, 0, s>>>(th, plan->tiles, bins,
-                                                                            base, pp, gate);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return launch_pass(*plan, false, keys, out, shift, base, nullptr, nullptr, th, status, gate, s,
-                     nullptr, 0);
-}
-
 cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
                              const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s) {
   if (radix_bits == 10)
     tile_hist_kernel<10><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc, nullptr,
-                                               tiles);
+                                               tiles, DigitAlt{});
   else
     tile_hist_kernel<8><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc, nullptr,
-                                              tiles);
+                                              tiles, DigitAlt{});
   return cudaGetLastError();
 }
 
