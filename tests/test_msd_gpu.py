@@ -44,6 +44,26 @@ def test_msd_form_even_cloud_with_duplicates():
     _check(pts, 1, "grid")
 
 
+def test_msd_form_heavy_duplicates():
+    # 64^3 cell centres: every bucket holds ~4,000 keys but only ~256 codes
+    rng = np.random.default_rng(6)
+    n = MIN_N + 4321
+    pts = np.ones((n, 4), np.float32)
+    pts[:, :3] = (rng.integers(0, 64, (n, 3)) * 16 + 8).astype(np.float32)
+    _check(pts, 1, "coarse grid")
+
+
+def test_msd_form_with_empty_buckets():
+    # x in the lower half of the box: the top-digit buckets of the upper half
+    # stay empty, the others hold twice the mean
+    rng = np.random.default_rng(8)
+    n = MIN_N + 99
+    pts = np.ones((n, 4), np.float32)
+    pts[:, 0] = rng.uniform(0, 512, n)
+    pts[:, 1:3] = rng.uniform(0, 1024, (n, 2))
+    _check(pts, 1, "half box")
+
+
 def test_msd_form_even_cloud():
     n = MIN_N + 1
     _check(O.init_random_vec4(n, 0.0, 1024.0, seed=77), 1, "uniform")
