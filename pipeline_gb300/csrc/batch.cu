@@ -582,7 +582,7 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
   cudaError_t e = cudaMemsetAsync(w, 0, P->zero_bytes, s);
   if (e != cudaSuccess) return batch_fail(e, "batch: clear");
   if (P->N > 0) {
-    const int mgrid = std::max(1, std::min(B.Ts, sms * 4));
+    const int mgrid = std::max(1, std::min(B.Ts, sms * 8));
     const size_t msm = 4 * (size_t)passes * bins;
     if (rb == 10) {
       batch_morton_kernel<10><<<mgrid, 256, msm, s>>>(reinterpret_cast<const float4*>(points), ka,
