@@ -203,18 +203,32 @@ __global__ void __launch_bounds__(256)
   __shared__ uint32_t s_total;
   __shared__ int s_max[8];
   __shared__ int s_hi;
-  const int tid = threadIdx.x;
   constexpr int ITEMS = 16;
+  // the tile's counts, then its prefix sums, staged so that global accesses
+  // are coalesced and each thread still scans 16 consecutive entries (padded:
+  // entry j at j + j / 32, conflict-free both ways)
+  __shared__ int s_v[256 * ITEMS + 256 * ITEMS / 32];
+  const int tid = threadIdx.x;
   const int t = blockIdx.x;
   const int4 d = B.tiles4k[t];
   const int c = d.z, cs = B.start[c];
   const int n = max(unique_c[c] - 1, 0);  // radix nodes of this cloud
   const int lo = d.x - cs;                // first node of the tile (cloud-local)
   if (lo >= n) return;
+  const int valid = min(256 * ITEMS, n - lo);
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int j = k * 256 + tid;
+    s_v[j + (j >> 5)] = j < valid ? ec[cs + lo + j] : 0;
+  }
+  __syncthreads();
   const int j0 = lo + tid * ITEMS;
   int v[ITEMS];
 #pragma unroll
-  for (int k = 0; k < ITEMS; ++k) v[k] = j0 + k < n ? ec[cs + j0 + k] : 0;
+  for (int k = 0; k < ITEMS; ++k) {
+    const int j = tid * ITEMS + k;
+    v[k] = s_v[j + (j >> 5)];
+  }
   uint32_t sum = 0;
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) sum += (uint32_t)v[k];
@@ -226,12 +240,19 @@ __global__ void __launch_bounds__(256)
   for (int k = 0; k < ITEMS; ++k) {
     const int i = j0 + k;
     run += (uint32_t)v[k];
+    const int j = tid * ITEMS + k;
+    s_v[j + (j >> 5)] = (int)run;  // each thread rewrites only its own entries
     if (i < n) {
-      ps_out[cs + i] = (int)run;
       const int last = v[k] > 0 ? (int)run + v[k] - 1 : (int)run;
       if (i > 0 && v[k] > 0 && last > mx) mx = last;
       if (i == n - 1 && (int)run > mx) mx = (int)run;
     }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int j = k * 256 + tid;
+    if (j < valid) ps_out[cs + lo + j] = s_v[j + (j >> 5)];
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -582,7 +603,7 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
   cudaError_t e = cudaMemsetAsync(w, 0, P->zero_bytes, s);
   if (e != cudaSuccess) return batch_fail(e, "batch: clear");
   if (P->N > 0) {
-    const int mgrid = std::max(1, std::min(B.Ts, sms * 8));
+    const int mgrid = std::max(1, std::min(B.Ts, sms * 16));
     const size_t msm = 4 * (size_t)passes * bins;
     if (rb == 10) {
       batch_morton_kernel<10><<<mgrid, 256, msm, s>>>(reinterpret_cast<const float4*>(points), ka,
