@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(256, 6)
 }
 
 // One CTA per 256 OctNode slots of a cloud.
-__global__ void __launch_bounds__(kFinThreads, 5)
+__global__ void __launch_bounds__(kFinThreads, 6)
     batch_oct_finalize_kernel(BatchDev B, BatchOctDev O) {
   __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
   const int4 d = B.slot_tiles[blockIdx.x];
