@@ -586,7 +586,19 @@ __global__ void __launch_bounds__(kUdThreads)
   }
   int cnt = 0;
   const int j0 = K.lo + tid * kUdItems;
-  if (j0 < K.hi) {
+  if ((reinterpret_cast<uintptr_t>(keys + K.lo) & 15) != 0) {
+    // Unaligned tile (a cloud starting mid-vector): warp-striped loads of
+    // each key and the one before it, coalesced, instead of 16 scalar
+    // strided loads per thread.
+#pragma unroll 4
+    for (int q = 0; q < kUdItems; ++q) {
+      const int j = K.lo + q * kUdThreads + tid;
+      if (j < K.hi) {
+        const uint32_t k = keys[j];
+        cnt += (j == K.cs) || k != keys[j - 1];
+      }
+    }
+  } else if (j0 < K.hi) {
     uint32_t prev = j0 > K.cs ? keys[j0 - 1] : 0u;
     uint32_t k[kUdItems];
     if (j0 + kUdItems <= K.hi && (reinterpret_cast<uintptr_t>(keys + j0) & 15) == 0) {
