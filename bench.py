@@ -487,6 +487,22 @@ def profile_only(args):
     from pipeline_gb300.pipeline import OctreeBuilder
 
     n = int(args.points)
+    if args.profile_only == "batched":
+        # the 512-cloud batch of the batched_512 workload (--points unused)
+        from pipeline_gb300 import datasets
+        from pipeline_gb300.batch import BatchOctreeBuilder
+
+        clouds = datasets.batched(512, seed=11)
+        sizes = [len(c) for c in clouds]
+        pts = torch.from_numpy(np.concatenate(clouds, 0)).cuda()
+        mins = torch.zeros(len(clouds), dtype=torch.float32, device="cuda")
+        ranges = torch.full((len(clouds),), RANGE, dtype=torch.float32, device="cuda")
+        bb = BatchOctreeBuilder(sizes)
+        for _ in range(max(args.warmup, 0) + 1):
+            bb.build(pts, mins, ranges)
+        torch.cuda.synchronize()
+        print(f"profile build (batched): {len(sizes)} clouds, {sum(sizes)} points")
+        return 0
     if args.profile_only == "learned":
         # clustered cloud of n points, model fit on 2^18 of its Morton codes
         from pipeline_gb300 import datasets
@@ -821,7 +837,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the clustered (learned) and batched workloads")
-    ap.add_argument("--profile-only", nargs="?", const="plain", choices=["plain", "learned"],
+    ap.add_argument("--profile-only", nargs="?", const="plain",
+                    choices=["plain", "learned", "batched"],
                     help="warm-up builds plus one build, no timing or output (for ncu captures)")
     ap.add_argument("--points", type=int, default=N_POINTS,
                     help="cloud size for --profile-only (smaller cases for multi-pass ncu captures)")
