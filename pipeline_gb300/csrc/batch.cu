@@ -381,6 +381,14 @@ __global__ void __launch_bounds__(kFinThreads, 6)
   __syncthreads();
   int* dst = reinterpret_cast<int*>(O.nodes + d.x);
   const int words = count * kNodeWords;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0 && (words & 3) == 0) {
+    // one bulk copy of the staged block (the TMA engine writes it)
+    if (threadIdx.x == 0) {
+      bulk_store_s2g(dst, s_nodes, (uint32_t)words * 4u);
+      bulk_wait_all();
+    }
+    return;
+  }
   int k0 = 0;
   if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
     const int quads = words >> 2;

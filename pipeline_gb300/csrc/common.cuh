@@ -73,6 +73,26 @@ __device__ __forceinline__ float4 ld_stream_f4(const float4* p) {
   return v;
 }
 
+// Bulk (TMA engine) copy of `bytes` from shared to global memory, issued by
+// one thread: both addresses 16-byte aligned, bytes a multiple of 16. The
+// fence makes the block's ordinary shared-memory stores (ordered by a
+// preceding barrier) visible to the copy; wait_read returns once the source
+// may be overwritten, wait_all once the writes are done.
+__device__ __forceinline__ void bulk_store_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(s),
+               "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 __device__ __forceinline__ void backoff(uint32_t it) {
   if (it > 8) __nanosleep(64);
 }

@@ -91,17 +91,26 @@ __global__ void __launch_bounds__(kFinThreads, 6) oct_finalize_kernel(int mode, 
     // 256 nodes are 960 16-byte words; blk is a multiple of 256, so dst is
     // 16-byte aligned whenever the node array is.
     const int words = count * kNodeWords;
-    int k0 = 0;
-    if ((reinterpret_cast<uintptr_t>(a.nodes) & 15) == 0) {
-      const int quads = words >> 2;
-      const uint4* src4 = reinterpret_cast<const uint4*>(s_nodes);
-      uint4* dst4 = reinterpret_cast<uint4*>(dst);
-      for (int k = threadIdx.x; k < quads; k += kFinThreads) dst4[k] = src4[k];
-      k0 = quads << 2;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0 && (words & 3) == 0) {
+      // one bulk copy of the staged block (the TMA engine writes it)
+      if (threadIdx.x == 0) {
+        bulk_store_s2g(dst, s_nodes, (uint32_t)words * 4u);
+        bulk_wait_read();  // the stage is free for the next block
+      }
+    } else {
+      int k0 = 0;
+      if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        const int quads = words >> 2;
+        const uint4* src4 = reinterpret_cast<const uint4*>(s_nodes);
+        uint4* dst4 = reinterpret_cast<uint4*>(dst);
+        for (int k = threadIdx.x; k < quads; k += kFinThreads) dst4[k] = src4[k];
+        k0 = quads << 2;
+      }
+      for (int k = k0 + threadIdx.x; k < words; k += kFinThreads) dst[k] = s_nodes[k];
     }
-    for (int k = k0 + threadIdx.x; k < words; k += kFinThreads) dst[k] = s_nodes[k];
     __syncthreads();
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t* status,
