@@ -12,10 +12,11 @@
 //            launches, which take the top digit's shift, bases and split sums
 //            when the MSD flag is set, so bucket b holds the keys
 //            [b << 20, (b + 1) << 20) in any order;
-//   buckets  one CTA per SM walks the buckets: a 2^20-bit bitmap (128 KiB of shared memory)
-//            marks the bucket's keys; its set bits, read in order, are the
-//            bucket's sorted unique keys (duplicates mark the same bit),
-//            written over the front of the bucket's own range;
+//   buckets  one CTA per SM walks the buckets: a 2^20-bit bitmap (128 KiB of
+//            shared memory) marks the bucket's keys; its set bits, read in
+//            order, are the bucket's sorted unique keys (duplicates mark the
+//            same bit), staged behind the bitmap and written over the front
+//            of the bucket's own range;
 //   pack     a scan of the unique counts, then one CTA per bucket copies its
 //            run to its output offset with the delta of each code to the
 //            next (the radix tree's input) and lowers the minima of the tree
@@ -274,9 +275,10 @@ __device__ __forceinline__ void msd_pack_run(const uint32_t* __restrict__ keys, 
     if (s_tmin[k] < kTtAbsent) atomic_min_u8(S.tile_min + t0 + k, s_tmin[k]);
 }
 
-// CTAs walk the buckets: a run goes to the codes from its output offset, with
-// each code's delta to the next one (the next bucket's first code after the
-// run's last) and the touched tree tiles' minima.
+// A CTA per bucket (the loop serves any grid): a run goes to the codes from
+// its output offset, with each code's delta to the next one (the next
+// bucket's first code after the run's last) and the touched tree tiles'
+// minima.
 __global__ void __launch_bounds__(kPackThreads)
     msd_pack_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ top_base,
                     const uint32_t* __restrict__ ucount, const uint32_t* __restrict__ uoff,
@@ -311,8 +313,7 @@ cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const u
   }
   uint32_t* ucount = static_cast<uint32_t*>(scratch);
   const int grid = std::min(kMsdBuckets, device_sm_count());  // one CTA fits an SM
-  msd_bucket_kernel<<<grid, kMsdThreads, smem, s>>>(keys, top_base, top_hist, ucount, gate,
-                                                           status);
+  msd_bucket_kernel<<<grid, kMsdThreads, smem, s>>>(keys, top_base, top_hist, ucount, gate, status);
   return cudaGetLastError();
 }
 
