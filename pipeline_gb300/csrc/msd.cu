@@ -224,7 +224,7 @@ __device__ __forceinline__ void msd_pack_run(const uint32_t* __restrict__ keys, 
   for (uint32_t k = tid; k < nt; k += kPackThreads) s_tmin[k] = kTtAbsent;
   __syncthreads();
   const uint32_t lane = tid & 31, warp = tid >> 5;
-  constexpr uint32_t kRows = 4;  // a warp takes 4 x 32 consecutive codes per round
+  constexpr uint32_t kRows = 8;  // a warp takes 8 x 32 consecutive codes per round
   constexpr uint32_t kSpan = kRows * 32;
   // whole warps iterate together (the shuffles and warp minima need every lane)
   for (uint32_t j0 = warp * kSpan; j0 < u; j0 += (kPackThreads / 32) * kSpan) {
@@ -238,7 +238,7 @@ __device__ __forceinline__ void msd_pack_run(const uint32_t* __restrict__ keys, 
     const uint32_t jn = j0 + kSpan;
     const uint32_t tail = jn < u ? src[jn] : after;
     uint32_t ma = kTtAbsent, mb = kTtAbsent;
-    const uint32_t ta = (o0 + j0) / kTtTile;  // the round's 128 positions: one tile or two
+    const uint32_t ta = (o0 + j0) / kTtTile;  // the round's 256 positions: one tile or two
 #pragma unroll
     for (uint32_t q = 0; q < kRows; ++q) {
       const uint32_t j = j0 + q * 32 + lane;
