@@ -352,6 +352,30 @@ def test_build_degenerate_sizes():
             assert b.result()["oct_nodes"].tobytes() == e["oct_nodes"].tobytes()
 
 
+def test_build_unaligned_node_array():
+    """OctNodes written to an array that is not 16-byte aligned (one node, 60
+    bytes, into an allocation): finalize takes its vector-store path instead
+    of the bulk copy, with the same bytes."""
+    import ctypes as C
+
+    from pipeline_gb300 import _lib
+
+    pts = O.init_random_vec4(30000, 0.0, 1024.0, seed=21)
+    expect = O.build_all(pts, 0.0, 1024.0)
+    b = _builder(len(pts))
+    shifted = torch.zeros((b.cap + 1, 15), dtype=torch.int32, device="cuda")
+    out = _lib.OctBuildOutputs.from_buffer_copy(b._out)
+    out.nodes = shifted.data_ptr() + 60  # 60 % 16 = 12
+    rc = b.lib.oct_build_octree(C.c_void_p(dev(pts).data_ptr()), len(pts), 0.0, 1024.0,
+                                C.byref(out), C.c_void_p(b.workspace.data_ptr()),
+                                b.workspace.numel(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "oct_build_octree")
+    c = b.counts()
+    assert (c.n_unique, c.n_oct, c.status) == (expect["n_unique"], expect["n_oct"], 0)
+    got = shifted[1:1 + c.n_oct].cpu().numpy()
+    assert got.tobytes() == expect["oct_nodes"].tobytes()
+
+
 def test_build_capacity_status():
     from pipeline_gb300 import _lib
 
