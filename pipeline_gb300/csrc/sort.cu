@@ -424,30 +424,40 @@ __global__ void __launch_bounds__(256)
   }
   constexpr int BINS = 1 << RB;
   __shared__ uint32_t h[BINS];
-  for (int b = threadIdx.x; b < BINS; b += 256) h[b] = 0;
-  __syncthreads();
-  const int t = blockIdx.x;
-  const int lo = tdesc ? tdesc[t].x : t * tile_keys;
-  const int hi = tdesc ? tdesc[t].y : min(n, lo + tile_keys);
-  const bool vec = ((reinterpret_cast<uintptr_t>(keys + lo)) & 15u) == 0;
-  const int n4 = vec ? (hi - lo) >> 2 : 0;
-  const uint4* k4 = reinterpret_cast<const uint4*>(keys + lo);
-  for (int i = threadIdx.x; i < n4; i += 256) {
-    const uint4 v = __ldcs(k4 + i);
-    atomicAdd(&h[(v.x >> shift) & (BINS - 1)], 1u);
-    atomicAdd(&h[(v.y >> shift) & (BINS - 1)], 1u);
-    atomicAdd(&h[(v.z >> shift) & (BINS - 1)], 1u);
-    atomicAdd(&h[(v.w >> shift) & (BINS - 1)], 1u);
+  // CTAs walk the tiles (a capped grid: a gated-off launch schedules few CTAs)
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+    for (int b = threadIdx.x; b < BINS; b += 256) h[b] = 0;
+    __syncthreads();
+    const int lo = tdesc ? tdesc[t].x : t * tile_keys;
+    const int hi = tdesc ? tdesc[t].y : min(n, lo + tile_keys);
+    const bool vec = ((reinterpret_cast<uintptr_t>(keys + lo)) & 15u) == 0;
+    const int n4 = vec ? (hi - lo) >> 2 : 0;
+    const uint4* k4 = reinterpret_cast<const uint4*>(keys + lo);
+    for (int i = threadIdx.x; i < n4; i += 256) {
+      const uint4 v = __ldcs(k4 + i);
+      atomicAdd(&h[(v.x >> shift) & (BINS - 1)], 1u);
+      atomicAdd(&h[(v.y >> shift) & (BINS - 1)], 1u);
+      atomicAdd(&h[(v.z >> shift) & (BINS - 1)], 1u);
+      atomicAdd(&h[(v.w >> shift) & (BINS - 1)], 1u);
+    }
+    for (int i = lo + 4 * n4 + threadIdx.x; i < hi; i += 256)
+      atomicAdd(&h[(keys[i] >> shift) & (BINS - 1)], 1u);
+    __syncthreads();
+    for (int b = threadIdx.x; b < BINS; b += 256) th[(size_t)t * BINS + b] = h[b];
+    if (part) {
+      uint32_t* ps = part + (size_t)(t / split_tiles(tiles)) * BINS;
+      for (int b = threadIdx.x; b < BINS; b += 256)
+        if (h[b]) atomicAdd(ps + b, h[b]);
+    }
+    __syncthreads();  // h is the next tile's
   }
-  for (int i = lo + 4 * n4 + threadIdx.x; i < hi; i += 256)
-    atomicAdd(&h[(keys[i] >> shift) & (BINS - 1)], 1u);
-  __syncthreads();
-  for (int b = threadIdx.x; b < BINS; b += 256) th[(size_t)t * BINS + b] = h[b];
-  if (part) {
-    uint32_t* ps = part + (size_t)(t / split_tiles(tiles)) * BINS;
-    for (int b = threadIdx.x; b < BINS; b += 256)
-      if (h[b]) atomicAdd(ps + b, h[b]);
-  }
+}
+
+// Grid of the tile-histogram kernel of the gated whole-build passes: the
+// tiles, capped at 8 CTAs per SM.
+static int tile_hist_grid(int tiles) {
+  const int cap = device_sm_count() * 8;
+  return tiles < cap ? tiles : cap;
 }
 
 // In place: th[t][b] becomes the output index where tile t's keys of digit b
@@ -684,10 +694,10 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
     if (plan->cfg.scan == 1) {
       uint32_t* pp = part + (size_t)p * kScanSplits * plan->bins;
       if (plan->radix_bits == 10)
-        tile_hist_kernel<10><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
+        tile_hist_kernel<10><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
                                                          nullptr, pp, plan->tiles, da);
       else
-        tile_hist_kernel<8><<<plan->tiles, 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
+        tile_hist_kernel<8><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
                                                         nullptr, pp, plan->tiles, da);
       tile_scan_split_kernel<<<dim3((plan->bins + 31) / 32, kScanSplits), 1024, 0, s>>>(
           th, plan->tiles, plan->bins, base + p * plan->bins, pp, g, da);

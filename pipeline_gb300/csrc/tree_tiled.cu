@@ -570,66 +570,70 @@ struct CloudKeys {
 // sums and smallest deltas.
 template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
-    unique_count_kernel(const uint32_t* __restrict__ keys, Map map, TreeScratch S,
+    unique_count_kernel(const uint32_t* __restrict__ keys, Map map, int n_tiles, TreeScratch S,
                         const uint32_t* __restrict__ gate) {
   if (gate && *gate == 0) return;
   __shared__ int s_cnt[kUdThreads / 32];
-  const int t = blockIdx.x, tid = threadIdx.x;
-  const KeyTile K = map(t);
-  if (t == 0) {
-    const int pad = (int)align_up((size_t)S.tiles, kTtMinBlock);
-    for (int k = S.tiles + tid; k < pad; k += kUdThreads) S.tile_min[k] = (uint8_t)kTtAbsent;
-  }
-  if (tid == 0) {
-    S.tile_min[t] = (uint8_t)kTtAbsent;
-    S.tile_sum[t] = 0;
-  }
-  int cnt = 0;
-  const int j0 = K.lo + tid * kUdItems;
-  if ((reinterpret_cast<uintptr_t>(keys + K.lo) & 15) != 0) {
-    // Unaligned tile (a cloud starting mid-vector): warp-striped loads of
-    // each key and the one before it, coalesced, instead of 16 scalar
-    // strided loads per thread.
+  const int tid = threadIdx.x;
+  // CTAs walk the tiles (a capped grid: a gated-off launch schedules few CTAs)
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const KeyTile K = map(t);
+    if (t == 0) {
+      const int pad = (int)align_up((size_t)S.tiles, kTtMinBlock);
+      for (int k = S.tiles + tid; k < pad; k += kUdThreads) S.tile_min[k] = (uint8_t)kTtAbsent;
+    }
+    if (tid == 0) {
+      S.tile_min[t] = (uint8_t)kTtAbsent;
+      S.tile_sum[t] = 0;
+    }
+    int cnt = 0;
+    const int j0 = K.lo + tid * kUdItems;
+    if ((reinterpret_cast<uintptr_t>(keys + K.lo) & 15) != 0) {
+      // Unaligned tile (a cloud starting mid-vector): warp-striped loads of
+      // each key and the one before it, coalesced, instead of 16 scalar
+      // strided loads per thread.
 #pragma unroll 4
-    for (int q = 0; q < kUdItems; ++q) {
-      const int j = K.lo + q * kUdThreads + tid;
-      if (j < K.hi) {
-        const uint32_t k = keys[j];
-        cnt += (j == K.cs) || k != keys[j - 1];
+      for (int q = 0; q < kUdItems; ++q) {
+        const int j = K.lo + q * kUdThreads + tid;
+        if (j < K.hi) {
+          const uint32_t k = keys[j];
+          cnt += (j == K.cs) || k != keys[j - 1];
+        }
+      }
+    } else if (j0 < K.hi) {
+      uint32_t prev = j0 > K.cs ? keys[j0 - 1] : 0u;
+      uint32_t k[kUdItems];
+      if (j0 + kUdItems <= K.hi && (reinterpret_cast<uintptr_t>(keys + j0) & 15) == 0) {
+#pragma unroll
+        for (int q = 0; q < kUdItems / 4; ++q) {
+          const uint4 v = reinterpret_cast<const uint4*>(keys + j0)[q];
+          k[4 * q] = v.x;
+          k[4 * q + 1] = v.y;
+          k[4 * q + 2] = v.z;
+          k[4 * q + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < kUdItems; ++q) k[q] = j0 + q < K.hi ? keys[j0 + q] : 0u;
+      }
+#pragma unroll
+      for (int q = 0; q < kUdItems; ++q) {
+        if (j0 + q < K.hi) {
+          cnt += (j0 + q == K.cs) || k[q] != prev;
+          prev = k[q];
+        }
       }
     }
-  } else if (j0 < K.hi) {
-    uint32_t prev = j0 > K.cs ? keys[j0 - 1] : 0u;
-    uint32_t k[kUdItems];
-    if (j0 + kUdItems <= K.hi && (reinterpret_cast<uintptr_t>(keys + j0) & 15) == 0) {
 #pragma unroll
-      for (int q = 0; q < kUdItems / 4; ++q) {
-        const uint4 v = reinterpret_cast<const uint4*>(keys + j0)[q];
-        k[4 * q] = v.x;
-        k[4 * q + 1] = v.y;
-        k[4 * q + 2] = v.z;
-        k[4 * q + 3] = v.w;
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < kUdItems; ++q) k[q] = j0 + q < K.hi ? keys[j0 + q] : 0u;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+    if ((tid & 31) == 0) s_cnt[tid >> 5] = cnt;
+    __syncthreads();
+    if (tid == 0) {
+      int total = 0;
+      for (int w = 0; w < kUdThreads / 32; ++w) total += s_cnt[w];
+      S.tile_heads[t] = total;
     }
-#pragma unroll
-    for (int q = 0; q < kUdItems; ++q) {
-      if (j0 + q < K.hi) {
-        cnt += (j0 + q == K.cs) || k[q] != prev;
-        prev = k[q];
-      }
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
-  if ((tid & 31) == 0) s_cnt[tid >> 5] = cnt;
-  __syncthreads();
-  if (tid == 0) {
-    int total = 0;
-    for (int w = 0; w < kUdThreads / 32; ++w) total += s_cnt[w];
-    S.tile_heads[t] = total;
+    __syncthreads();  // s_cnt is the next tile's
   }
 }
 
@@ -640,7 +644,7 @@ __global__ void __launch_bounds__(kUdThreads)
 template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
     unique_deltas_kernel(const uint32_t* __restrict__ keys, Map map, uint32_t* __restrict__ out,
-                         TreeScratch S, int* __restrict__ unique_c,
+                         int n_tiles, TreeScratch S, int* __restrict__ unique_c,
                          const uint32_t* __restrict__ gate) {
   if (gate && *gate == 0) return;
   __shared__ uint32_t s_keys[kTtTile + kTtTile / 32];
@@ -648,83 +652,93 @@ __global__ void __launch_bounds__(kUdThreads)
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ uint32_t s_min[2][kUdThreads / 32];
-  const int t = blockIdx.x, tid = threadIdx.x;
-  const KeyTile K = map(t);
-  const int valid = K.hi - K.lo;
-  if (valid <= 0) return;
+  const int tid = threadIdx.x;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const KeyTile K = map(t);
+    const int valid = K.hi - K.lo;
+    if (valid <= 0) continue;  // uniform in the CTA
 #pragma unroll 4
-  for (int j = tid; j < kTtTile; j += kUdThreads) {
-    const int idx = K.lo + j;
-    s_keys[ud_pad(j)] = j < valid ? keys[idx] : 0u;
-  }
-  const uint32_t before = K.lo > K.cs ? keys[K.lo - 1] : 0u;
-  __syncthreads();
-  uint32_t key[kUdItems], dk[kUdItems];
-  uint32_t flags = 0;
-  int cnt = 0;
-  const int j0 = tid * kUdItems;
-  uint32_t prev = j0 == 0 ? before : s_keys[ud_pad(j0 - 1)];
-#pragma unroll
-  for (int k = 0; k < kUdItems; ++k) {
-    key[k] = s_keys[ud_pad(j0 + k)];
-    const int j = j0 + k;
-    const bool head = j < valid && ((K.lo + j == K.cs) || key[k] != prev);
-    dk[k] = tt_delta(prev, key[k]);  // used for heads past the cloud's first code only
-    flags |= (uint32_t)head << k;
-    cnt += head;
-    prev = key[k];
-  }
-  const uint32_t off = block_exclusive_sum<kUdThreads>((uint32_t)cnt, s_warp, &s_total);
-  const uint32_t total = s_total;
-  const uint32_t base = S.tile_upos[t] - S.tile_upos[K.t_first];
-  // Stage the heads (s_keys is free after the scan's barriers) and their deltas.
-  uint32_t o = off;
-#pragma unroll
-  for (int k = 0; k < kUdItems; ++k) {
-    if (flags >> k & 1u) {
-      s_keys[ud_pad(o)] = key[k];
-      s_d[o] = (uint8_t)dk[k];
-      ++o;
+    for (int j = tid; j < kTtTile; j += kUdThreads) {
+      const int idx = K.lo + j;
+      s_keys[ud_pad(j)] = j < valid ? keys[idx] : 0u;
     }
-  }
-  __syncthreads();
-  // Deltas go to positions base - 1 .. base + total - 2 (the cloud's first code
-  // has none), i.e. the cloud's tree tiles ta and at most ta + 1.
-  const int first = base == 0 ? 1 : 0;
-  const int ta = (int)(base + first - 1) / kTtTile;
-  uint32_t ma = kTtAbsent, mb = kTtAbsent;
-  for (int j = tid; j < (int)total; j += kUdThreads) {
-    out[K.cs + base + j] = s_keys[ud_pad(j)];
-    if (j >= first) {
-      const int pos = (int)base + j - 1;
-      const uint32_t d = s_d[j];
-      S.D[(size_t)(K.t_first + pos / kTtTile) * kTtTile + pos % kTtTile] = (uint8_t)d;
-      if (pos / kTtTile == ta) ma = min(ma, d);
-      else mb = min(mb, d);
-    }
-  }
+    const uint32_t before = K.lo > K.cs ? keys[K.lo - 1] : 0u;
+    __syncthreads();
+    uint32_t key[kUdItems], dk[kUdItems];
+    uint32_t flags = 0;
+    int cnt = 0;
+    const int j0 = tid * kUdItems;
+    uint32_t prev = j0 == 0 ? before : s_keys[ud_pad(j0 - 1)];
 #pragma unroll
-  for (int sh = 16; sh > 0; sh >>= 1) {
-    ma = min(ma, __shfl_xor_sync(kFull, ma, sh));
-    mb = min(mb, __shfl_xor_sync(kFull, mb, sh));
-  }
-  if ((tid & 31) == 0) {
-    s_min[0][tid >> 5] = ma;
-    s_min[1][tid >> 5] = mb;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    if ((int)total > first) {
-      uint32_t a = kTtAbsent, b = kTtAbsent;
-      for (int w = 0; w < kUdThreads / 32; ++w) {
-        a = min(a, s_min[0][w]);
-        b = min(b, s_min[1][w]);
+    for (int k = 0; k < kUdItems; ++k) {
+      key[k] = s_keys[ud_pad(j0 + k)];
+      const int j = j0 + k;
+      const bool head = j < valid && ((K.lo + j == K.cs) || key[k] != prev);
+      dk[k] = tt_delta(prev, key[k]);  // used for heads past the cloud's first code only
+      flags |= (uint32_t)head << k;
+      cnt += head;
+      prev = key[k];
+    }
+    const uint32_t off = block_exclusive_sum<kUdThreads>((uint32_t)cnt, s_warp, &s_total);
+    const uint32_t total = s_total;
+    const uint32_t base = S.tile_upos[t] - S.tile_upos[K.t_first];
+    // Stage the heads (s_keys is free after the scan's barriers) and their deltas.
+    uint32_t o = off;
+#pragma unroll
+    for (int k = 0; k < kUdItems; ++k) {
+      if (flags >> k & 1u) {
+        s_keys[ud_pad(o)] = key[k];
+        s_d[o] = (uint8_t)dk[k];
+        ++o;
       }
-      if (a < kTtAbsent) atomic_min_u8(S.tile_min + K.t_first + ta, a);
-      if (b < kTtAbsent) atomic_min_u8(S.tile_min + K.t_first + ta + 1, b);
     }
-    if (unique_c && K.last) unique_c[K.cloud] = (int)(base + total);
+    __syncthreads();
+    // Deltas go to positions base - 1 .. base + total - 2 (the cloud's first code
+    // has none), i.e. the cloud's tree tiles ta and at most ta + 1.
+    const int first = base == 0 ? 1 : 0;
+    const int ta = (int)(base + first - 1) / kTtTile;
+    uint32_t ma = kTtAbsent, mb = kTtAbsent;
+    for (int j = tid; j < (int)total; j += kUdThreads) {
+      out[K.cs + base + j] = s_keys[ud_pad(j)];
+      if (j >= first) {
+        const int pos = (int)base + j - 1;
+        const uint32_t d = s_d[j];
+        S.D[(size_t)(K.t_first + pos / kTtTile) * kTtTile + pos % kTtTile] = (uint8_t)d;
+        if (pos / kTtTile == ta) ma = min(ma, d);
+        else mb = min(mb, d);
+      }
+    }
+#pragma unroll
+    for (int sh = 16; sh > 0; sh >>= 1) {
+      ma = min(ma, __shfl_xor_sync(kFull, ma, sh));
+      mb = min(mb, __shfl_xor_sync(kFull, mb, sh));
+    }
+    if ((tid & 31) == 0) {
+      s_min[0][tid >> 5] = ma;
+      s_min[1][tid >> 5] = mb;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      if ((int)total > first) {
+        uint32_t a = kTtAbsent, b = kTtAbsent;
+        for (int w = 0; w < kUdThreads / 32; ++w) {
+          a = min(a, s_min[0][w]);
+          b = min(b, s_min[1][w]);
+        }
+        if (a < kTtAbsent) atomic_min_u8(S.tile_min + K.t_first + ta, a);
+        if (b < kTtAbsent) atomic_min_u8(S.tile_min + K.t_first + ta + 1, b);
+      }
+      if (unique_c && K.last) unique_c[K.cloud] = (int)(base + total);
+    }
+    __syncthreads();  // the shared arrays are the next tile's
   }
+}
+
+// Grid of the whole build's (gated) unique kernels: the tiles, capped at 8
+// CTAs per SM.
+static int unique_grid(int tiles) {
+  const int cap = device_sm_count() * 8;
+  return tiles < cap ? tiles : cap;
 }
 
 cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_out, int* d_unique,
@@ -732,12 +746,13 @@ cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_
   if (n <= 0) return cudaMemsetAsync(d_unique, 0, sizeof(int), s);
   const TreeScratch S = tree_scratch_carve(tree_scratch, n);
   const OneKeys map{n};
-  unique_count_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, S, gate);
+  unique_count_kernel<<<unique_grid(S.tiles), kUdThreads, 0, s>>>(sorted, map, S.tiles, S, gate);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
     e = launch_tile_counts_scan(S.tiles, S.tile_heads, S.tile_upos, d_unique, s, gate);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<S.tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, nullptr, gate);
+  unique_deltas_kernel<<<unique_grid(S.tiles), kUdThreads, 0, s>>>(sorted, map, codes_out, S.tiles, S,
+                                                                   nullptr, gate);
   return cudaGetLastError();
 }
 
@@ -747,11 +762,12 @@ cudaError_t launch_batch_unique_deltas(const uint32_t* sorted, const int4* tiles
   if (n_tiles <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
   const CloudKeys map{tiles, n_tiles, start};
-  unique_count_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, S, nullptr);
+  unique_count_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, n_tiles, S, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = launch_tile_counts_scan(n_tiles, S.tile_heads, S.tile_upos, nullptr, s);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, S, unique_c, nullptr);
+  unique_deltas_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, n_tiles, S,
+                                                                   unique_c, nullptr);
   return cudaGetLastError();
 }
 
