@@ -82,3 +82,32 @@ def test_lsd_fallback_for_uneven_cloud():
 def test_below_msd_size_uses_lsd():
     n = MIN_N - 1
     _check(O.init_random_vec4(n, 0.0, 1024.0, seed=3), 0, "below")
+
+
+def test_captured_build_takes_either_form():
+    # One captured graph, replayed over an even cloud (MSD branch) and then,
+    # with the points changed in place, over a clustered one (LSD branch) and
+    # back: the branch is chosen on the device at every replay.
+    from pipeline_gb300.pipeline import OctreeBuilder
+
+    n = MIN_N + 333
+    even = O.init_random_vec4(n, 0.0, 1024.0, seed=21)
+    rng = np.random.default_rng(22)
+    c = rng.uniform(100, 900, (5, 3))
+    idx = rng.integers(0, 5, n)
+    clustered = np.ones((n, 4), np.float32)
+    clustered[:, :3] = np.clip(rng.normal(c[idx], 10.0), 0, np.nextafter(np.float32(1024), 0))
+    d_pts = torch.from_numpy(np.ascontiguousarray(even)).cuda()
+    b = OctreeBuilder(n)
+    b.capture(d_pts, 0.0, 1024.0)
+    for pts, form in ((even, 1), (clustered, 2), (even, 1)):
+        d_pts.copy_(torch.from_numpy(np.ascontiguousarray(pts)))
+        b.nodes.fill_(-1)
+        b.replay()
+        res = b.result()
+        assert b.sort_form() == form
+        expect = O.build_all(pts, 0.0, 1024.0)
+        assert (res["n_unique"], res["n_oct"], res["status"]) == \
+            (expect["n_unique"], expect["n_oct"], 0), form
+        for key in STAGES:
+            assert res[key].tobytes() == np.asarray(expect[key]).tobytes(), (form, key)
