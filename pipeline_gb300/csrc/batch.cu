@@ -378,6 +378,7 @@ __global__ void __launch_bounds__(kFinThreads, 6)
   if ((int)threadIdx.x < count)
     finalize_slot(true, p, a, cloud_tags(O, z), a.prefix_n[0] / 3,
                   s_nodes + threadIdx.x * kNodeWords);
+  bulk_fence_writes();
   __syncthreads();
   int* dst = reinterpret_cast<int*>(O.nodes + d.x);
   const int words = count * kNodeWords;

@@ -78,6 +78,12 @@ __device__ __forceinline__ float4 ld_stream_f4(const float4* p) {
 // fence makes the block's ordinary shared-memory stores (ordered by a
 // preceding barrier) visible to the copy; wait_read returns once the source
 // may be overwritten, wait_all once the writes are done.
+// Every thread that wrote shared memory a bulk copy will read runs this
+// before the barrier that precedes the copy: its generic-proxy writes are
+// then ordered before the async proxy's reads.
+__device__ __forceinline__ void bulk_fence_writes() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ void bulk_store_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
   const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

@@ -121,6 +121,7 @@ __device__ __forceinline__ void msd_bucket(uint32_t* __restrict__ keys, uint32_t
     if (lane >= o) inc += t;
   }
   if (lane == 31) s_wsum[w] = inc;
+  if (tid == 0) bulk_wait_read();  // the previous bucket's copy has read the stage
   __syncthreads();
   uint32_t pos = inc - own, total = 0;
 #pragma unroll 8
@@ -135,11 +136,13 @@ __device__ __forceinline__ void msd_bucket(uint32_t* __restrict__ keys, uint32_t
   // (kMsdStage keys), else written straight out. `total` is the same in
   // every thread, so the branch is uniform. A lane walks its own set bits in
   // one loop (words re-read from the bitmap), so a warp runs as many rounds
-  // as its fullest lane has keys.
+  // as its fullest lane has keys. The stage starts at the run's offset
+  // within its 16-byte word, so the run's 16-byte words are the stage's.
   uint32_t* out = keys + lo;
+  const uint32_t sh = lo & 3u;
   uint32_t* stage = bm + kMsdWords;
   const bool staged = total <= (uint32_t)kMsdStage;
-  uint32_t* dst = staged ? stage : out;
+  uint32_t* dst = staged ? stage + sh : out;
   const uint32_t kc = ((uint32_t)b << kMsdSpanBits) | ((uint32_t)c << 10);
   uint32_t bits = 0, kw = 0;
   for (uint32_t e = 0; e < own; ++e) {
@@ -154,8 +157,15 @@ __device__ __forceinline__ void msd_bucket(uint32_t* __restrict__ keys, uint32_t
     dst[pos + e] = kw | (uint32_t)bit;
   }
   if (staged) {
+    bulk_fence_writes();
     __syncthreads();
-    for (uint32_t i = tid; i < total; i += kMsdThreads) out[i] = stage[i];
+    // the aligned middle as one bulk copy (the TMA engine writes it while the
+    // CTA goes on to the next bucket's bitmap), the ragged ends by threads
+    const uint32_t h0 = min((4u - sh) & 3u, total);
+    const uint32_t mid = (total - h0) & ~3u;
+    if (tid == 0 && mid > 0) bulk_store_s2g(out + h0, stage + sh + h0, mid * 4u);
+    if (tid < h0) out[tid] = stage[sh + tid];
+    for (uint32_t i = h0 + mid + tid; i < total; i += kMsdThreads) out[i] = stage[sh + i];
   }
 }
 
@@ -171,8 +181,9 @@ __global__ void __launch_bounds__(kMsdThreads, 1)
   // one CTA per SM (its shared memory) walks the buckets
   for (int b = blockIdx.x; b < kMsdBuckets; b += gridDim.x) {
     msd_bucket(keys, top_base[b], top_hist[b], b, bm, s_wsum, ucount, status, tid, lane, w);
-    __syncthreads();  // the next bucket clears the bitmap and the stage
+    __syncthreads();  // the next bucket clears the bitmap
   }
+  if (tid == 0) bulk_wait_all();  // the runs are written before the kernel ends
 }
 
 __global__ void __launch_bounds__(kMsdBuckets)
@@ -303,7 +314,7 @@ cudaError_t launch_msd_gate(const uint32_t* top_hist, int n, uint32_t* flags, cu
 cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const uint32_t* top_hist,
                                void* scratch, const uint32_t* gate, uint32_t* status,
                                cudaStream_t s) {
-  constexpr int smem = sizeof(uint32_t) * (kMsdWords + kMsdStage);
+  constexpr int smem = sizeof(uint32_t) * (kMsdWords + kMsdStage + 4);  // + the stage's shift
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(msd_bucket_kernel,

@@ -86,6 +86,7 @@ __global__ void __launch_bounds__(kFinThreads, 6) oct_finalize_kernel(int mode, 
     const int p = blk + threadIdx.x;
     const int count = min(kFinThreads, z.n_oct - blk);
     if (p < z.n_oct) finalize_slot(fresh, p, a, t, root_level, s_nodes + threadIdx.x * kNodeWords);
+    bulk_fence_writes();
     __syncthreads();
     int* dst = out_words + (size_t)blk * kNodeWords;
     // 256 nodes are 960 16-byte words; blk is a multiple of 256, so dst is
