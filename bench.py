@@ -732,7 +732,7 @@ def sort_bar_workload(dev, flush, reps, pts):
     16,777,216 Morton codes (30-bit, device-resident, one sort per rep)."""
     import torch
 
-    from pipeline_gb300 import _lib, build as native
+    from pipeline_gb300 import _lib
     from pipeline_gb300.kernels import _workspace, k_ComputeMortonCode
 
     n = pts.shape[0]
@@ -771,7 +771,9 @@ def sort_bar_workload(dev, flush, reps, pts):
     out = {"workload": "sort stage: 16,777,216 30-bit Morton codes of the uniform cloud, "
                        "device-resident", "ours_ms": round(t_ours, 4),
            "ours_gkeys_s": round(n / t_ours / 1e6, 2), "ours_sorted": bool(ok_ours)}
-    path = native.build_bar()
+    from cub_bar import build as cub_bar
+
+    path = cub_bar.build()
     if path is None:
         out["cub"] = "unavailable: CUB did not build"
         return out

@@ -1,7 +1,7 @@
 // Comparison bar for the sort stage: CUB's DeviceRadixSort::SortKeys on the
 // same keys (the library sort the reference benchmarks against,
-// benchmarks/cuda/bm_02_sort.cuh:117-140). Built into its own library, used
-// only by bench.py; no product path links it.
+// benchmarks/cuda/bm_02_sort.cuh:117-140). Built by cub_bar/build.py into its
+// own library, used only by bench.py; no product path links it.
 #include <cub/device/device_radix_sort.cuh>
 #include <cuda_runtime.h>
 #include <stdint.h>

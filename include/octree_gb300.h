@@ -115,6 +115,13 @@ OCT_API const char* oct_last_error(void);
 /* ----------------------------------------------------------------------- */
 OCT_API void oct_init_random_vec4(oct_vec4* out, int n, float min_coord, float range, int seed);
 
+/* Stage 0 (device): key sequences. Replace k_InitDescending and            */
+/* k_InitAscending (include/kernels/00_init.hpp:5-7, kernels/00_init.cpp:5-17)*/
+/* : keys[i] = n - i, or keys[i] = i, for i in [0, n). d_keys: DEVICE       */
+/* pointer. Asynchronous on `stream`.                                        */
+OCT_API int oct_init_descending(uint32_t* d_keys, int n, oct_stream_t stream);
+OCT_API int oct_init_ascending(uint32_t* d_keys, int n, oct_stream_t stream);
+
 /* Stage 0 (device): the reference's device generator gpu::k_InitRandomVec4  */
 /* (include/cuda/kernels/00_init.cuh:7-8, kernels/cuda/00_init.cu:11-50) as  */
 /* its driver launches it (apps/gpu_demo/main.cu:168-175, one element per    */
@@ -151,8 +158,11 @@ OCT_API int oct_sort_keys(uint32_t* keys, uint32_t* keys_alt, int n, int key_bit
  * a fixed 6.5 MiB __device__ array inside the library, which every GPU that
  * loads the library holds until exit. n above OCT_NOALLOC_SORT_MAX_KEYS
  * returns OCT_ERR_TOO_LARGE. The first call on a device sets up the array's
- * address; make it before any stream capture. Calls share the array: calls
- * that overlap on the GPU race. */
+ * address; make it before any stream capture. The address is kept for the
+ * life of the process, so cudaDeviceReset on that device after the first
+ * call is not supported. Several devices in one process are supported (each
+ * gets its own array). Calls share the array: calls that overlap on the GPU
+ * race. */
 #define OCT_NOALLOC_SORT_MAX_KEYS (1 << 22)
 #define OCT_NOALLOC_SORT_SCRATCH_BYTES (6815744u)
 OCT_API int oct_sort_keys_noalloc(uint32_t* keys, uint32_t* keys_alt, int n, int key_bits,
@@ -411,6 +421,25 @@ OCT_API int oct_check_tree(const oct_node* nodes, int n_nodes, const uint32_t* c
                            uint32_t root_prefix, int root_code_len, int root_index,
                            long long* d_counts, void* workspace, size_t workspace_bytes,
                            oct_stream_t stream);
+
+/* ----------------------------------------------------------------------- */
+/* Diagnostics: bounded look-back waits. No counterpart in the reference,    */
+/* whose look-back spins have no bound (kernels/cuda/02_sort.cu:461-479).    */
+/* Every look-back wait of this library gives up after 1 s without its flag, */
+/* sets OCT_STATUS_SPIN_TIMEOUT in the status word and lets its kernel       */
+/* return. This call runs one such wait on a tile whose predecessor never    */
+/* publishes (the workspace is cleared first), with the bound limit_ns (at   */
+/* most 1 s), so a caller can check that it returns within that time with   */
+/* the bit set. which: OCT_DIAG_WAIT_SORT (the sort's per-digit look-back)   */
+/* or OCT_DIAG_WAIT_SCAN (the warp look-back of unique and prefix sum).      */
+/* workspace: DEVICE, 256-byte aligned, oct_diag_wait_workspace_bytes().     */
+/* ----------------------------------------------------------------------- */
+#define OCT_DIAG_WAIT_SORT 0
+#define OCT_DIAG_WAIT_SCAN 1
+OCT_API size_t oct_diag_wait_workspace_bytes(void);
+OCT_API int oct_diag_lookback_timeout(int which, unsigned long long limit_ns, void* workspace,
+                                      size_t workspace_bytes, uint32_t* d_status,
+                                      oct_stream_t stream);
 
 #ifdef __cplusplus
 } /* extern "C" */

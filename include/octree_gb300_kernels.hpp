@@ -117,6 +117,22 @@ inline int oct_node_count(const int* counts, const int* offsets, int n) {
 
 }  // namespace octree_gb300_detail
 
+// include/kernels/00_init.hpp:5 (keys[i] = n - i).
+inline void k_InitDescending(unsigned int* sort, int n) {
+  namespace d = octree_gb300_detail;
+  d::DeviceView<unsigned int> out(sort, n > 0 ? (size_t)n : 0, false);
+  d::oct_ok(oct_init_descending(out.get(), n, nullptr), "k_InitDescending");
+  out.copy_out();
+}
+
+// include/kernels/00_init.hpp:7 (keys[i] = i).
+inline void k_InitAscending(unsigned int* sort, int n) {
+  namespace d = octree_gb300_detail;
+  d::DeviceView<unsigned int> out(sort, n > 0 ? (size_t)n : 0, false);
+  d::oct_ok(oct_init_ascending(out.get(), n, nullptr), "k_InitAscending");
+  out.copy_out();
+}
+
 // include/kernels/00_init.hpp:10-11 (host generator).
 template <class Vec4>
 inline void k_InitRandomVec4(Vec4* u_data, int n, float min, float range, int seed) {

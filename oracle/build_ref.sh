@@ -33,3 +33,25 @@ SRCS=(
 g++ -std=c++17 -O2 -fopenmp -ffp-contract=off $ARCHFLAGS -fPIC -shared \
   -I "$HERE/glm_shim" -I "$REF/include" "${SRCS[@]}" -o "$OUT/libref.so"
 echo "built $OUT/libref.so"
+# The reference's checkTree (apps/cpu_demo/main.cpp:13-35), compiled from the
+# unmodified demo with its main renamed and CLI11 / spdlog served by the
+# stand-ins in oracle/ref_check/, driven by oracle/ref_check_main.cpp.
+g++ -std=c++17 -O2 -fopenmp -ffp-contract=off $ARCHFLAGS \
+  -Dmain=ref_demo_main -I "$HERE/ref_check" -I "$HERE/glm_shim" -I "$REF/include" \
+  -c "$REF/apps/cpu_demo/main.cpp" -o "$OUT/cpu_demo_main.o"
+g++ -std=c++17 -O2 -fopenmp -ffp-contract=off $ARCHFLAGS \
+  -I "$HERE/glm_shim" -I "$REF/include" "$HERE/ref_check_main.cpp" "$OUT/cpu_demo_main.o" \
+  "${SRCS[@]:0:8}" -o "$OUT/ref_check"
+echo "built $OUT/ref_check"
+# The reference's device generator gpu::k_InitRandomVec4
+# (kernels/cuda/00_init.cu), compiled unmodified for sm_103a into a cubin that
+# tests/golden/make_device_init.py loads and launches on a GB300 the way
+# apps/gpu_demo/main.cu:168-175 does (the cubin is built here, where the
+# reference sources are, and run where the GPU is).
+NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+if [ -x "$NVCC" ]; then
+  "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -O3 --expt-relaxed-constexpr \
+    -I "$HERE/glm_shim" -I "$REF/include" "$REF/kernels/cuda/00_init.cu" \
+    -o "$OUT/init_ref.sm_103a.cubin"
+  echo "built $OUT/init_ref.sm_103a.cubin"
+fi

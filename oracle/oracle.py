@@ -114,6 +114,8 @@ def load_ref():
             sig = {
                 "ref_set_threads": (None, [C.c_int]),
                 "ref_init_random_vec4": (None, [P, C.c_int, C.c_float, C.c_float, C.c_int]),
+                "ref_init_descending": (None, [P, C.c_int]),
+                "ref_init_ascending": (None, [P, C.c_int]),
                 "ref_morton": (None, [P, P, C.c_long, C.c_float, C.c_float]),
                 "ref_radix_sort": (None, [P, C.c_int]),
                 "ref_radix_sort_alt": (None, [P, P, C.c_int]),

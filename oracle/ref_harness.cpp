@@ -7,6 +7,8 @@
 // under tests/golden/. Nothing in the product links or loads it.
 //
 // Reference interfaces wrapped (paths within the reference project):
+//   k_InitDescending      include/kernels/00_init.hpp:5, kernels/00_init.cpp:6-11
+//   k_InitAscending       include/kernels/00_init.hpp:7, kernels/00_init.cpp:13-18
 //   k_InitRandomVec4      include/kernels/00_init.hpp:10-11, kernels/00_init.cpp:20-30
 //   k_ComputeMortonCode   include/kernels/01_morton.hpp:9-13
 //   k_SimpleRadixSort     include/kernels/02_sort.hpp:6-7
@@ -32,6 +34,10 @@ static_assert(sizeof(OctNode) == 60, "OctNode is 60 bytes");
 extern "C" {
 
 void ref_set_threads(int n) { omp_set_num_threads(n); }
+
+void ref_init_descending(unsigned* keys, int n) { k_InitDescending(keys, n); }
+
+void ref_init_ascending(unsigned* keys, int n) { k_InitAscending(keys, n); }
 
 void ref_init_random_vec4(float* out, int n, float min, float range, int seed) {
   k_InitRandomVec4(reinterpret_cast<glm::vec4*>(out), n, min, range, seed);

@@ -28,6 +28,9 @@ OCT_STATUS_CAPACITY = 8
 
 OCT_MAX_N = (1 << 30) - 1
 
+OCT_DIAG_WAIT_SORT = 0
+OCT_DIAG_WAIT_SCAN = 1
+
 _STATUS_NAMES = {
     OCT_ERR_INVALID_ARG: "invalid argument",
     OCT_ERR_WORKSPACE: "workspace too small",
@@ -96,6 +99,8 @@ SIGNATURES = {
     "oct_build_workspace_bytes": (Z, [I, I]),
     "oct_build_octree": (I, [P, I, F, F, C.POINTER(OctBuildOutputs), P, Z, P]),
     "oct_read_counts": (I, [P, P, P]),
+    "oct_init_descending": (I, [P, I, P]),
+    "oct_init_ascending": (I, [P, I, P]),
     "oct_init_random_vec4_device": (I, [P, I, F, F, I, P]),
     "oct_morton_decode": (I, [P, I, F, F, P, P]),
     "oct_check_tree_workspace_bytes": (Z, [I]),
@@ -122,6 +127,8 @@ SIGNATURES = {
     "oct_build_step_count": (I, []),
     "oct_build_step_name": (C.c_char_p, [I]),
     "oct_build_octree_timed": (I, [P, I, F, F, C.POINTER(OctBuildOutputs), P, Z, P, I, P]),
+    "oct_diag_wait_workspace_bytes": (Z, []),
+    "oct_diag_lookback_timeout": (I, [I, C.c_ulonglong, P, Z, P, P]),
 }
 
 _lock = threading.Lock()

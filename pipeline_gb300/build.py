@@ -86,27 +86,5 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB_PATH
 
 
-BAR_SRC = os.path.join(PKG, "bar", "cub_sort.cu")
-BAR_LIB = os.path.join(OUT_DIR, "libpipeline_gb300_cubbar.so")
-
-
-def build_bar(force: bool = False, verbose: bool = False) -> str | None:
-    """The CUB comparison bar used by bench.py (its own library; not part of
-    the product). Returns its path, or None when CUB does not build here."""
-    if not force and not _stale(BAR_LIB, [BAR_SRC, os.path.abspath(__file__)]):
-        return BAR_LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
-    tmp = BAR_LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc(), *ARCH_FLAGS, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-cudart",
-           "static", BAR_SRC, "-o", tmp]
-    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
-    if r.returncode != 0:
-        if verbose:
-            sys.stdout.write(r.stdout.decode(errors="replace"))
-        return None
-    os.replace(tmp, BAR_LIB)
-    return BAR_LIB
-
-
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose="--verbose" in sys.argv)

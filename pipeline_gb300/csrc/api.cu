@@ -493,6 +493,27 @@ int oct_build_octree_timed(const oct_vec4* points, int n, float min_coord, float
 
 
 
+size_t oct_diag_wait_workspace_bytes(void) { return 2 * 1024 * sizeof(uint32_t); }
+
+int oct_diag_lookback_timeout(int which, unsigned long long limit_ns, void* workspace,
+                              size_t workspace_bytes, uint32_t* d_status, oct_stream_t stream) {
+  if ((which != OCT_DIAG_WAIT_SORT && which != OCT_DIAG_WAIT_SCAN) || limit_ns == 0 ||
+      limit_ns > kWaitLimitNs || !workspace || !aligned(workspace, 256) || !d_status)
+    return OCT_ERR_INVALID_ARG;
+  if (workspace_bytes < oct_diag_wait_workspace_bytes()) return OCT_ERR_WORKSPACE;
+  cudaStream_t s = S(stream);
+  // Every look-back word starts unpublished; nothing publishes tile 0.
+  OCT_TRY(cudaMemsetAsync(workspace, 0, oct_diag_wait_workspace_bytes(), s), "oct_diag: clear");
+  if (which == OCT_DIAG_WAIT_SORT)
+    OCT_TRY(launch_diag_sort_wait(static_cast<uint32_t*>(workspace), d_status, limit_ns, s),
+            "oct_diag_lookback_timeout");
+  else
+    OCT_TRY(launch_diag_scan_wait(static_cast<unsigned long long*>(workspace), d_status, limit_ns,
+                                  s),
+            "oct_diag_lookback_timeout");
+  return OCT_OK;
+}
+
 int oct_read_counts(const int32_t* d_counts, int32_t* h_counts, oct_stream_t stream) {
   if (!d_counts || !h_counts) return OCT_ERR_INVALID_ARG;
   cudaStream_t s = S(stream);

@@ -38,6 +38,14 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Key sequences of kernels/00_init.cpp:5-17: keys[i] = n - i (descending) or
+// i (ascending), as unsigned 32-bit values.
+__global__ void __launch_bounds__(256)
+    init_sequence_kernel(uint32_t* __restrict__ keys, int n, int descending) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    keys[i] = descending ? (uint32_t)(n - i) : (uint32_t)i;
+}
+
 // ------------------------------------------------------------------ decode --
 __global__ void __launch_bounds__(256)
     morton_decode_kernel(const uint32_t* __restrict__ codes, int n, float min_coord, float range,
@@ -178,6 +186,30 @@ OCT_API int oct_init_random_vec4_device(oct_vec4* d_points, int n, float min_coo
     return OCT_ERR_CUDA;
   }
   return OCT_OK;
+}
+
+static int init_sequence(uint32_t* d_keys, int n, int descending, oct_stream_t stream) {
+  using namespace octgb;
+  if (n < 0 || (n > 0 && !d_keys)) return OCT_ERR_INVALID_ARG;
+  if (n == 0) return OCT_OK;
+  int grid = (n + 255) / 256;
+  if (grid > device_sm_count() * 16) grid = device_sm_count() * 16;
+  init_sequence_kernel<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(d_keys, n,
+                                                                                descending);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e));
+    return OCT_ERR_CUDA;
+  }
+  return OCT_OK;
+}
+
+OCT_API int oct_init_descending(uint32_t* d_keys, int n, oct_stream_t stream) {
+  return init_sequence(d_keys, n, 1, stream);
+}
+
+OCT_API int oct_init_ascending(uint32_t* d_keys, int n, oct_stream_t stream) {
+  return init_sequence(d_keys, n, 0, stream);
 }
 
 OCT_API int oct_morton_decode(const uint32_t* codes, int n, float min_coord, float range,

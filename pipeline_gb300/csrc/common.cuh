@@ -12,9 +12,14 @@ constexpr uint32_t kStatusWalkLimit = 2u;    // a parent walk exceeded its bound
 constexpr uint32_t kStatusRange = 4u;        // a coordinate outside [min, min + range]
 constexpr uint32_t kStatusCapacity = 8u;     // octree node capacity too small
 
-// A look-back poll costs an L2 round trip plus a 64 ns sleep after the first
-// few misses, so this bound ends a wait that never completes in about a second.
-constexpr uint32_t kSpinLimit = 1u << 21;
+// Look-back waits are bounded in time: a wait that has not seen the flag it
+// polls after kWaitLimitNs of %globaltimer gives up, sets the status bit and
+// lets its kernel return (no wait lasts longer than this, and a build in
+// which one gave up reports OCT_STATUS_SPIN_TIMEOUT instead of hanging).
+// kWaitPollCap also ends a wait after that many polls (at least 64 ns each)
+// should the timer not advance.
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+constexpr uint32_t kWaitPollCap = 1u << 26;
 
 constexpr int kWarp = 32;
 
@@ -99,9 +104,32 @@ __device__ __forceinline__ void bulk_wait_all() {
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-__device__ __forceinline__ void backoff(uint32_t it) {
-  if (it > 8) __nanosleep(64);
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
+
+// Bound of one wait. expired() is called after every poll that did not find
+// its flag: it backs off (64 ns sleeps after the first few polls), reads the
+// timer on the first poll and every 32nd after it, and returns true once
+// limit_ns have passed since the first poll (or after kWaitPollCap polls).
+struct WaitBound {
+  unsigned long long limit_ns;
+  unsigned long long t0 = 0;
+  uint32_t polls = 0;
+  __device__ __forceinline__ explicit WaitBound(unsigned long long limit) : limit_ns(limit) {}
+  __device__ __forceinline__ bool expired() {
+    ++polls;
+    if (polls > 8) __nanosleep(64);
+    if ((polls & 31u) == 1u) {
+      const unsigned long long now = global_ns();
+      if (polls == 1u) t0 = now;
+      else if (now - t0 > limit_ns) return true;
+    }
+    return polls > kWaitPollCap;
+  }
+};
 
 __device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bit) {
   if (status) atomicOr(status, bit);

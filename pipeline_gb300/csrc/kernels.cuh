@@ -29,10 +29,29 @@ static inline void mark(Recorder* r, cudaStream_t s) {
   if (r) r->mark(s);
 }
 
+// SM count of the current device (cached per device).
 int device_sm_count();
+
+// Raises func's dynamic shared-memory limit to at least `bytes` on the
+// current device (once per device and kernel; kernel attributes are per
+// device context).
+cudaError_t set_smem_limit(const void* func, int bytes);
+template <typename F>
+static inline cudaError_t set_smem_limit(F* func, int bytes) {
+  return set_smem_limit(reinterpret_cast<const void*>(func), bytes);
+}
 
 // Sets the text oct_last_error() returns on this thread.
 void set_last_error(const char* msg);
+
+// ---- diagnostics ---------------------------------------------------------
+// One look-back wait on a tile whose predecessor never publishes (the sort's
+// digit look-back over 2 x 1024 words, or the unique / prefix-sum warp
+// look-back over 2 words), bounded by limit_ns.
+cudaError_t launch_diag_sort_wait(uint32_t* lookback, uint32_t* status,
+                                  unsigned long long limit_ns, cudaStream_t s);
+cudaError_t launch_diag_scan_wait(unsigned long long* lb, uint32_t* status,
+                                  unsigned long long limit_ns, cudaStream_t s);
 
 // ---- sort ----------------------------------------------------------------
 // Tunable shape of the radix sort (chosen by the autotuner or the default).

@@ -404,12 +404,7 @@ cudaError_t launch_lcdf_fit(const uint32_t* sorted_sample, int S, int k_req, int
   int grid = (S + 255) / 256;
   if (grid > device_sm_count() * 4) grid = device_sm_count() * 4;
   if (grid < 1) grid = 1;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(lcdf_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         12 * (kLcdfMaxSegments + 1));
-    attr = true;
-  }
+  set_smem_limit(lcdf_fwd_bwd_kernel, 12 * (kLcdfMaxSegments + 1));
   for (int it = 0; it < steps; ++it) {
     lcdf_prep_kernel<<<1, 1024, 0, s>>>(blob, L);
     lcdf_fwd_bwd_kernel<<<grid, 256, fb_smem, s>>>(sorted_sample, S, blob, L);
@@ -426,8 +421,7 @@ cudaError_t launch_lcdf_fit(const uint32_t* sorted_sample, int S, int k_req, int
 cudaError_t launch_lcdf_train(const uint32_t* sorted_sample, int S, int steps, float lr, char* blob,
                               const LcdfLayout& L, cudaStream_t s) {
   const size_t fb_smem = 12 * (size_t)(L.max_knots + 1);
-  cudaFuncSetAttribute(lcdf_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       12 * (kLcdfMaxSegments + 1));
+  set_smem_limit(lcdf_fwd_bwd_kernel, 12 * (kLcdfMaxSegments + 1));
   int grid = (S + 255) / 256;
   if (grid > device_sm_count() * 4) grid = device_sm_count() * 4;
   if (grid < 1) grid = 1;
@@ -442,12 +436,7 @@ cudaError_t launch_lcdf_train(const uint32_t* sorted_sample, int S, int steps, f
 cudaError_t launch_lcdf_loss_grad(const uint32_t* sorted_sample, int S, char* blob,
                                   const LcdfLayout& L, float* grad_out, cudaStream_t s) {
   const size_t fb_smem = 12 * (size_t)(L.max_knots + 1);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(lcdf_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         12 * (kLcdfMaxSegments + 1));
-    attr = true;
-  }
+  set_smem_limit(lcdf_fwd_bwd_kernel, 12 * (kLcdfMaxSegments + 1));
   int grid = (S + 255) / 256;
   if (grid > device_sm_count() * 4) grid = device_sm_count() * 4;
   if (grid < 1) grid = 1;
@@ -467,13 +456,8 @@ cudaError_t launch_lcdf_tables(char* blob, const LcdfLayout& L, int nb, cudaStre
 cudaError_t launch_lcdf_buckets(const char* blob, const LcdfLayout& L, const uint32_t* keys, int n,
                                 uint32_t* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  static bool attr = false;
   const size_t smem = lcdf_tables_smem(L.max_knots);
-  if (!attr) {
-    cudaFuncSetAttribute(lcdf_bucket_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)lcdf_tables_smem(kLcdfMaxSegments));
-    attr = true;
-  }
+  set_smem_limit(lcdf_bucket_kernel, (int)lcdf_tables_smem(kLcdfMaxSegments));
   int grid = (n + 255) / 256;
   if (grid > device_sm_count() * 8) grid = device_sm_count() * 8;
   lcdf_bucket_kernel<<<grid, 256, smem, s>>>(blob, L, keys, n, out);

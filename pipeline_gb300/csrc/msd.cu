@@ -315,13 +315,8 @@ cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const u
                                void* scratch, const uint32_t* gate, uint32_t* status,
                                cudaStream_t s) {
   constexpr int smem = sizeof(uint32_t) * (kMsdWords + kMsdStage + 4);  // + the stage's shift
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(msd_bucket_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  const cudaError_t e = set_smem_limit(msd_bucket_kernel, smem);
+  if (e != cudaSuccess) return e;
   uint32_t* ucount = static_cast<uint32_t*>(scratch);
   const int grid = std::min(kMsdBuckets, device_sm_count());  // one CTA fits an SM
   msd_bucket_kernel<<<grid, kMsdThreads, smem, s>>>(keys, top_base, top_hist, ucount, gate, status);

@@ -30,7 +30,8 @@ constexpr unsigned long long kLbFlags = 3ull << 62;
 // load (flag and value share a 64-bit word), so one round trip covers 32
 // predecessors. Returns the exclusive prefix in every lane; lane 0 publishes.
 __device__ uint32_t warp_lookback_u32(unsigned long long* lb, int tile, uint32_t agg,
-                                      uint32_t* status) {
+                                      uint32_t* status,
+                                      unsigned long long limit_ns = kWaitLimitNs) {
   const int lane = threadIdx.x & 31;
   if (tile == 0) {
     if (lane == 0) st_release_u64(lb, kLbInc | agg);
@@ -39,7 +40,7 @@ __device__ uint32_t warp_lookback_u32(unsigned long long* lb, int tile, uint32_t
   if (lane == 0) st_release_u64(lb + tile, kLbAgg | agg);
   uint32_t ex = 0;
   int pred = tile - 1;
-  uint32_t spins = 0;
+  WaitBound wait(limit_ns);
   while (true) {
     const int p = pred - lane;
     const unsigned long long w = p >= 0 ? ld_relaxed_u64(lb + p) : kLbInc;
@@ -51,11 +52,10 @@ __device__ uint32_t warp_lookback_u32(unsigned long long* lb, int tile, uint32_t
     if (first_nr < first_inc) {  // take the ready words before it, wait on it
       ex += __reduce_add_sync(0xffffffffu, lane < first_nr ? (uint32_t)w : 0u);
       pred -= first_nr;
-      if (++spins > kSpinLimit) {
+      if (__any_sync(0xffffffffu, wait.expired())) {  // the warp leaves together
         if (lane == 0) raise_status(status, kStatusSpinTimeout);
         break;
       }
-      backoff(spins);
       continue;
     }
     const int take = first_inc < 32 ? first_inc + 1 : 32;
@@ -65,6 +65,19 @@ __device__ uint32_t warp_lookback_u32(unsigned long long* lb, int tile, uint32_t
   }
   if (lane == 0) st_release_u64(lb + tile, kLbInc | (uint32_t)(ex + agg));
   return ex;
+}
+
+// Diagnostics: the warp look-back of tile 1 whose predecessor (tile 0) never
+// publishes; it must give up after limit_ns with the status bit set.
+__global__ void diag_warp_wait_kernel(unsigned long long* lb, uint32_t* status,
+                                      unsigned long long limit_ns) {
+  warp_lookback_u32(lb, 1, 1u, status, limit_ns);
+}
+
+cudaError_t launch_diag_scan_wait(unsigned long long* lb, uint32_t* status,
+                                  unsigned long long limit_ns, cudaStream_t s) {
+  diag_warp_wait_kernel<<<1, 32, 0, s>>>(lb, status, limit_ns);
+  return cudaGetLastError();
 }
 
 // --------------------------------------------------------------------------

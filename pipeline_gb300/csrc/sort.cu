@@ -14,6 +14,11 @@
 // the keys in shared memory in digit order and scatters them in runs.
 // 30-bit Morton keys take 3 passes of 10-bit digits (28 B/key of HBM traffic
 // including the histogram read) instead of the reference's 4 passes of 8.
+#include <atomic>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "kernels.cuh"
 
 namespace octgb {
@@ -155,6 +160,67 @@ constexpr uint32_t kValMask = (1u << 30) - 1;
 
 __device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
   asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Decoupled look-back for digit b of tile `tile` (> 0) over the per-tile words
+// lookback[t * BINS + b] (flag in the top two bits, count below): first probe
+// the immediate predecessor, then windows of kWin predecessor words (relaxed
+// loads, all in flight), summing aggregates until an inclusive word. Publishes
+// the tile's inclusive value and returns its exclusive prefix. A word that is
+// not published within limit_ns makes the wait give up (status bit set; the
+// prefix is then meaningless and the caller's scatter stays in bounds).
+template <int BINS>
+__device__ __forceinline__ uint32_t digit_lookback(uint32_t* lookback, int tile, int b,
+                                                  uint32_t own, uint32_t* status,
+                                                  unsigned long long limit_ns) {
+  constexpr int kWin = 16;
+  uint32_t prefix = 0;
+  int pred = tile - 1;
+  WaitBound wait(limit_ns);
+  bool done = false;
+  {
+    uint32_t w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
+    while ((w0 & kFlagMask) == 0) {
+      if (wait.expired()) {
+        raise_status(status, kStatusSpinTimeout);
+        done = true;
+        break;
+      }
+      w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
+    }
+    prefix += w0 & kValMask;
+    done = done || (w0 & kFlagMask) == kFlagInc;
+    --pred;
+  }
+  while (!done) {
+    uint32_t w[kWin];
+#pragma unroll
+    for (int k = 0; k < kWin; ++k)
+      w[k] = (pred - k >= 0) ? ld_relaxed_u32(lookback + (size_t)(pred - k) * BINS + b) : kFlagInc;
+    bool stop = false;
+    int adv = 0;
+#pragma unroll
+    for (int k = 0; k < kWin; ++k) {
+      const uint32_t f = w[k] & kFlagMask;
+      if (!stop) {
+        if (f == 0) {
+          stop = true;
+        } else {
+          prefix += w[k] & kValMask;
+          ++adv;
+          if (f == kFlagInc) stop = done = true;
+        }
+      }
+    }
+    if (done) break;
+    pred -= adv;
+    if (adv < kWin && wait.expired()) {  // stopped at a word not ready yet: poll it again
+      raise_status(status, kStatusSpinTimeout);
+      break;
+    }
+  }
+  st_relaxed_u32(lookback + (size_t)tile * BINS + b, kFlagInc | ((prefix + own) & kValMask));
+  return prefix;
 }
 
 template <int RB, int WARPS, int ITEMS, bool STABLE>
@@ -310,65 +376,13 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
     for (int b = tid; b < BINS; b += THREADS)
       bin_glob[b] = tile_prefix[(size_t)tile * BINS + b] - bin_local[b];
   } else {
-    // Decoupled look-back per digit: first probe the immediate predecessor,
-    // then windows of kWin predecessor words (relaxed loads, all in flight).
-    constexpr int kWin = 16;
+    // Decoupled look-back per digit (digit_lookback).
 #pragma unroll
     for (int j = 0; j < PER_T; ++j) {
       const int b = tid + j * THREADS;
       if (b >= BINS) break;
-      uint32_t prefix = 0;
-      if (tile > 0) {
-        int pred = tile - 1;
-        uint32_t spins = 0;
-        bool done = false;
-        {
-          uint32_t w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
-          while ((w0 & kFlagMask) == 0) {
-            if (++spins > kSpinLimit) {
-              raise_status(status, kStatusSpinTimeout);
-              break;
-            }
-            backoff(spins);
-            w0 = ld_relaxed_u32(lookback + (size_t)pred * BINS + b);
-          }
-          prefix += w0 & kValMask;
-          done = (w0 & kFlagMask) == kFlagInc || spins > kSpinLimit;
-          --pred;
-        }
-        while (!done) {
-          uint32_t w[kWin];
-#pragma unroll
-          for (int k = 0; k < kWin; ++k)
-            w[k] = (pred - k >= 0) ? ld_relaxed_u32(lookback + (size_t)(pred - k) * BINS + b)
-                                   : kFlagInc;
-          bool stop = false;
-          int adv = 0;
-#pragma unroll
-          for (int k = 0; k < kWin; ++k) {
-            const uint32_t f = w[k] & kFlagMask;
-            if (!stop) {
-              if (f == 0) {
-                stop = true;
-              } else {
-                prefix += w[k] & kValMask;
-                ++adv;
-                if (f == kFlagInc) stop = done = true;
-              }
-            }
-          }
-          if (done) break;
-          pred -= adv;
-          if (adv < kWin) {  // stopped at a word that is not ready yet: poll it again
-            if (++spins > kSpinLimit) {
-              raise_status(status, kStatusSpinTimeout);
-              break;
-            }
-            backoff(spins);
-          }
-        }
-        st_relaxed_u32(lookback + (size_t)tile * BINS + b, kFlagInc | ((prefix + own[j]) & kValMask));
-      }
+      const uint32_t prefix =
+          tile > 0 ? digit_lookback<BINS>(lookback, tile, b, own[j], status, kWaitLimitNs) : 0u;
       bin_glob[b] = bin_base[b] + prefix - bin_local[b];
     }
   }
@@ -544,15 +558,60 @@ SortPlan sort_plan_cfg(int n, int key_bits, SortConfig cfg) {
 
 SortPlan sort_plan(int n, int key_bits) { return sort_plan_cfg(n, key_bits, g_default_cfg); }
 
-static int g_num_sms = 0;
+// Per-device caches: the SM count, and the dynamic shared-memory limits
+// already raised (a kernel attribute belongs to one device's context).
+namespace {
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_num_sms[kMaxDevices];
+std::mutex g_attr_mu;
+std::vector<std::tuple<int, const void*, int>> g_attr_set;
+
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+  return dev;
+}
+}  // namespace
+
 int device_sm_count() {
-  if (g_num_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 152;
+  const int dev = current_device();
+  if (dev >= kMaxDevices) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 152;
   }
-  return g_num_sms;
+  int v = g_num_sms[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (v <= 0) v = 152;
+    g_num_sms[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+
+cudaError_t set_smem_limit(const void* func, int bytes) {
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lock(g_attr_mu);
+  for (const auto& t : g_attr_set)
+    if (std::get<0>(t) == dev && std::get<1>(t) == func && std::get<2>(t) >= bytes)
+      return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) g_attr_set.emplace_back(dev, func, bytes);
+  return e;
+}
+
+// Diagnostics: one digit look-back of tile 1 whose predecessor (tile 0) never
+// publishes; it must give up after limit_ns with the status bit set.
+__global__ void diag_digit_wait_kernel(uint32_t* lookback, uint32_t* status,
+                                       unsigned long long limit_ns) {
+  if (threadIdx.x == 0) digit_lookback<1024>(lookback, 1, 0, 1u, status, limit_ns);
+}
+
+cudaError_t launch_diag_sort_wait(uint32_t* lookback, uint32_t* status,
+                                  unsigned long long limit_ns, cudaStream_t s) {
+  diag_digit_wait_kernel<<<1, 32, 0, s>>>(lookback, status, limit_ns);
+  return cudaGetLastError();
 }
 
 template <int RB, int WARPS, int ITEMS, bool STABLE, int SCAN>
@@ -563,11 +622,8 @@ static cudaError_t launch_pass_t(const uint32_t* src, uint32_t* dst, int n, int 
                                  int tiles_override, DigitAlt alt) {
   using L = PassSmem<RB, WARPS, ITEMS, STABLE>;
   auto k = sort_pass_kernel<RB, WARPS, ITEMS, STABLE, SCAN>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
-    attr = true;
-  }
+  const cudaError_t ea = set_smem_limit(reinterpret_cast<const void*>(k), L::BYTES);
+  if (ea != cudaSuccess) return ea;
   const int tiles = tiles_override > 0 ? tiles_override : (n + L::TILE - 1) / L::TILE;
   k<<<tiles, WARPS * 32, L::BYTES, s>>>(src, dst, n, shift, base, lookback, counter, tile_prefix,
                                         status, gate, tdesc, alt);

@@ -17,7 +17,10 @@
 //    until the process exits.
 //  - Set-up: the first call on a device resolves the array's device address
 //    with cudaGetSymbolAddress while that device is current; make that first
-//    call before any stream capture on the device.
+//    call before any stream capture on the device. The address is kept for
+//    the life of the process: cudaDeviceReset on a device after its first
+//    call is not supported (the array would be reloaded at another address).
+//    Each device of a process has its own array and address.
 //  - Sharing: every call uses the same array and clears the part it needs at
 //    the start of the call. Calls that overlap on the GPU (on different
 //    streams, or from different host threads without ordering) race on it.

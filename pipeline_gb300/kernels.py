@@ -257,6 +257,19 @@ def k_LinkLeafNodes(nodes: torch.Tensor, node_offsets: torch.Tensor,
         _ptr(status, "status"), _stream()), "k_LinkLeafNodes")
 
 
+def k_InitDescending(sort: torch.Tensor, n: int) -> None:
+    """include/kernels/00_init.hpp:5: sort[i] = n - i (uint32 in an int32
+    CUDA tensor), on the current stream."""
+    _lib.check(_lib.load().oct_init_descending(_ptr(sort, "sort", torch.int32, n), n, _stream()),
+               "oct_init_descending")
+
+
+def k_InitAscending(sort: torch.Tensor, n: int) -> None:
+    """include/kernels/00_init.hpp:7: sort[i] = i, on the current stream."""
+    _lib.check(_lib.load().oct_init_ascending(_ptr(sort, "sort", torch.int32, n), n, _stream()),
+               "oct_init_ascending")
+
+
 # ------------------------------------------------------------ consumers --
 def k_InitRandomVec4_device(points: torch.Tensor, n: int, min_coord: float, rng: float,
                             seed: int) -> None:

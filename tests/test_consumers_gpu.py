@@ -102,3 +102,39 @@ def test_check_tree_finds_wrong_leaves_and_bad_links():
     got = check_tree(dev_nodes, m, b.codes, u, prefix, clen)
     assert got == want
     assert want[1] > 0 and want[2] > 0 and want[3] > 0
+
+
+@pytest.mark.parametrize("n", [1, 767, 100_003, 1 << 22])
+def test_init_sequences(n):
+    from pipeline_gb300.kernels import k_InitAscending, k_InitDescending
+
+    d = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    a = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    k_InitDescending(d, n)
+    k_InitAscending(a, n)
+    idx = np.arange(n, dtype=np.int64)
+    assert np.array_equal(d.cpu().numpy().view(np.uint32).astype(np.int64), n - idx)
+    assert np.array_equal(a.cpu().numpy().view(np.uint32).astype(np.int64), idx)
+
+
+def _device_init_fixture():
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "device_init.json")
+    if not os.path.exists(path):
+        return []
+    with open(path) as f:
+        return json.load(f)["cases"]
+
+
+@pytest.mark.parametrize("case", _device_init_fixture(), ids=lambda c: f'n{c["n"]}_seed{c["seed"]}')
+def test_device_generator_matches_reference_gpu_output(case):
+    """oct_init_random_vec4_device against the reference's own kernel's output
+    (kernels/cuda/00_init.cu run on a GB300: tests/golden/device_init.json)."""
+    from pipeline_gb300.kernels import k_InitRandomVec4_device
+
+    n = case["n"]
+    pts = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    k_InitRandomVec4_device(pts, n, case["min"], case["range"], case["seed"])
+    assert O.fnv1a64(pts.cpu().numpy()) == case["hash"]

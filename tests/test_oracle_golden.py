@@ -5,6 +5,9 @@ unmodified CPU stage functions (tests/golden/make_golden.py). Stage 8 of a case
 marked "o7" is not reference output (the reference never returns there); the
 oracle's contract value is checked against its own stage-7 prefix instead.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -137,3 +140,37 @@ def test_check_tree_restatement_small():
     nodes[2]["child_node_mask"] = 0b1000000
     nodes[2]["children"][6] = 9  # out of range
     assert O.check_tree(nodes, codes, 0, 0) == (3, 2, 1, 1)
+
+
+def test_init_sequences_match_reference():
+    """k_InitDescending / k_InitAscending (kernels/00_init.cpp:5-17): the
+    reference's own functions, where they are built here, give n - i and i."""
+    ref = O.load_ref()
+    if ref is None:
+        pytest.skip("the reference's CPU kernels are not built here")
+    for n in (0, 1, 10, 100_003):
+        d = np.full(max(n, 1), 0xDEADBEEF, np.uint32)
+        a = d.copy()
+        ref.ref_init_descending(d.ctypes.data, n)
+        ref.ref_init_ascending(a.ctypes.data, n)
+        assert d[:n].tolist() == (n - np.arange(n)).tolist()
+        assert a[:n].tolist() == np.arange(n).tolist()
+
+
+def _device_init_fixture():
+    path = os.path.join(os.path.dirname(__file__), "golden", "device_init.json")
+    if not os.path.exists(path):
+        return []
+    with open(path) as f:
+        return json.load(f)["cases"]
+
+
+@pytest.mark.parametrize("case", _device_init_fixture(),
+                         ids=lambda c: f'n{c["n"]}_seed{c["seed"]}')
+def test_device_generator_restatement_matches_reference_gpu_output(case):
+    """The oracle's restatement of gpu::k_InitRandomVec4 against the values the
+    reference's own kernel (kernels/cuda/00_init.cu, run on a GB300 as its
+    driver launches it) produced: tests/golden/device_init.json."""
+    got = O.init_random_vec4_gpu(case["n"], case["min"], case["range"], case["seed"])
+    assert got[:2].tolist() == case["first_points"][:case["n"]]
+    assert O.fnv1a64(got) == case["hash"]
