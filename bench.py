@@ -61,10 +61,8 @@ WORKLOAD = ("uniform_16m: 16,777,216 float32 points uniform in [0,1024)^3, seed 
 # writing 4 B per unique key, and the pack reading 4 B and writing 5 B per
 # unique key: code and delta); the radix tree with its edge counts reads 4 B
 # per code and writes 15 B per node (11 B of tree + 4 B of edge count); the
-# prefix sum reads 4 B and writes 4 B per node; octree: 40 B per radix node
-# read, 60 B per OctNode written and 4 B per leaf link, all in the tile
-# kernel (the fix-up pass, which rebuilds the ~1% of slots written across
-# tiles, has no algorithmic bytes of its own).
+# prefix sum reads 4 B and writes 4 B per node; octree: 40 B per radix node read, 60 B per OctNode written, 4 B per
+# leaf link (split over the emit and finalize launches).
 def algorithmic_bytes(n, u, b, m, msd=False):
     leaves = b + 1
     if msd:  # MSD form: pass 0's launches scatter on the top digit, bucket bitmaps, pack
@@ -77,7 +75,8 @@ def algorithmic_bytes(n, u, b, m, msd=False):
         **sort,
         "radix tree+edge count": 4 * u + 15 * b,
         "prefix sum": 8 * b,
-        "octree tiles": 40 * b + 4 * leaves + 60 * m,
+        "octree emit": 40 * b + 4 * leaves,
+        "octree finalize": 60 * m,
     }
 
 
@@ -466,7 +465,8 @@ def build_launches(n: int = 0) -> int:
     """Kernel launches of one plain build under the active sort shape:
     Morton, digit-base scan, per pass (tile histogram + tile scan +) pass,
     unique (run-head count, their scan, compaction with the deltas), tree
-    nodes, tile-sum scan + prefix sum, octree tiles + fix-up, counts."""
+    nodes, tile-sum scan + prefix sum (which clears the octree tags), octree
+    emit/finalize, counts."""
     from pipeline_gb300 import autotune
 
     rb, _, _, scan = autotune.get_config()
@@ -802,8 +802,8 @@ TRAFFIC_KERNELS = {"morton+histogram": ["morton_kernel<10, 1>"],
                    "unique": ["unique_count_kernel", "unique_deltas_kernel"],
                    "radix tree+edge count": ["tree_nodes_kernel"],
                    "prefix sum": ["tile_sums_scan_kernel", "edge_scan_kernel"],
-                   "octree tiles": ["oct_tile_kernel"],
-                   "octree fix-up": ["oct_fixup_kernel"]}
+                   "octree emit": ["oct_emit_kernel"],
+                   "octree finalize": ["oct_finalize_kernel"]}
 
 
 def read_traffic(kernel_step: str, n: int):

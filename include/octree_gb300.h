@@ -434,14 +434,6 @@ OCT_API int oct_check_tree(const oct_node* nodes, int n_nodes, const uint32_t* c
 /* or OCT_DIAG_WAIT_SCAN (the warp look-back of unique and prefix sum).      */
 /* workspace: DEVICE, 256-byte aligned, oct_diag_wait_workspace_bytes().     */
 /* ----------------------------------------------------------------------- */
-/* Tiling of the whole-build octree stage (no counterpart in the reference):  */
-/* radix nodes per tile (1-512) and octree slots per shared-memory pass       */
-/* (1-512) for later builds in this process; (0, 0) restores the default      */
-/* (512, 512). Smaller values only make more of the work go through the       */
-/* fix-up pass (writes across tiles) and the chunk loop; results are the      */
-/* same. For tests and tuning; not thread-safe against concurrent builds.     */
-OCT_API int oct_set_octree_tiling(int tile_nodes, int chunk_slots);
-
 #define OCT_DIAG_WAIT_SORT 0
 #define OCT_DIAG_WAIT_SCAN 1
 OCT_API size_t oct_diag_wait_workspace_bytes(void);

@@ -127,7 +127,6 @@ SIGNATURES = {
     "oct_build_step_count": (I, []),
     "oct_build_step_name": (C.c_char_p, [I]),
     "oct_build_octree_timed": (I, [P, I, F, F, C.POINTER(OctBuildOutputs), P, Z, P, I, P]),
-    "oct_set_octree_tiling": (I, [I, I]),
     "oct_diag_wait_workspace_bytes": (Z, []),
     "oct_diag_lookback_timeout": (I, [I, C.c_ulonglong, P, Z, P, P]),
 }

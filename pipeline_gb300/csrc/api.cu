@@ -32,8 +32,8 @@ cudaStream_t S(oct_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 struct BuildLayout {
   SortPlan sort;
   ScanPlan uniq;
-  size_t sort_off, uniq_off, misc_off, fix_off, ctrl_bytes;
-  size_t msd_off, keys_a_off, keys_b_off, tree_off, list_off, total;
+  size_t sort_off, uniq_off, misc_off, ctrl_bytes;
+  size_t msd_off, keys_a_off, keys_b_off, tree_off, tags_off, total;
 };
 
 BuildLayout build_layout(int n, int cap) {
@@ -45,15 +45,14 @@ BuildLayout build_layout(int n, int cap) {
   // histograms (always fully written before use) follow.
   L.uniq_off = 0;
   L.misc_off = align_up(L.uniq_off + L.uniq.bytes, 256);
-  L.fix_off = align_up(L.misc_off + 256, 256);
-  L.sort_off = align_up(L.fix_off + oct_fix_zero_bytes(cap), 256);
+  L.sort_off = align_up(L.misc_off + 256, 256);
   L.ctrl_bytes = L.sort_off + L.sort.zero_bytes;
   L.msd_off = align_up(L.sort_off + L.sort.bytes, 256);
   L.keys_a_off = align_up(L.msd_off + msd_scratch_bytes(), 256);
   L.keys_b_off = align_up(L.keys_a_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
   L.tree_off = align_up(L.keys_b_off + sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), 256);
-  L.list_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
-  L.total = align_up(L.list_off + oct_fix_list_bytes(cap), 256);
+  L.tags_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
+  L.total = align_up(L.tags_off + oct_tags_bytes(cap), 256);
   return L;
 }
 
@@ -409,8 +408,9 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
                                         w + L.tree_off, s),
           "build: radix tree");
   mark(rec, s);
+  const OctTags tags = oct_tags_carve(w + L.tags_off, out->nodes_capacity);
   OCT_TRY(launch_prefix_sum_clear_tags(n, m.unique, out->edge_count, out->prefix_sum, m.max_slot,
-                                       w + L.tree_off, m.status, OctTags{}, s),
+                                       w + L.tree_off, m.status, tags, s),
           "build: prefix sum");
   mark(rec, s);
   if (out->nodes_capacity > 0) {
@@ -430,8 +430,8 @@ static int build_impl(const oct_vec4* points, int n, float min_coord, float rang
     a.n_brt_host = n;
     a.d_unique = m.unique;
     a.d_max_slot = m.max_slot;
-    const OctFix fix = oct_fix_carve(w + L.fix_off, w + L.list_off, out->nodes_capacity);
-    OCT_TRY(launch_octree_tiled(a, fix, m.status, s, rec), "build: octree");
+    OCT_TRY(launch_octree(kOctMake | kOctLink | kOctFresh, a, tags, m.status, s, rec, true),
+            "build: octree");
   } else {
     for (int k = 0; k < 2; ++k) mark(rec, s);
   }
@@ -451,8 +451,8 @@ int oct_build_octree(const oct_vec4* points, int n, float min_coord, float range
 static const char* const kBuildSteps[] = {
     "start",       "clear",       "morton+histogram", "histogram scan",
     "sort pass 0", "sort pass 1", "sort pass 2",      "msd buckets",
-    "unique",      "radix tree+edge count", "prefix sum", "octree tiles",
-    "octree fix-up", "publish counts"};
+    "unique",      "radix tree+edge count", "prefix sum", "octree emit",
+    "octree finalize", "publish counts"};
 
 int oct_build_sort_form(const void* workspace, int n, int nodes_capacity, int* form) {
   if (!workspace || !form || n < 0 || n > OCT_MAX_N || nodes_capacity < 0)
@@ -492,10 +492,6 @@ int oct_build_octree_timed(const oct_vec4* points, int n, float min_coord, float
 }
 
 
-
-int oct_set_octree_tiling(int tile_nodes, int chunk_slots) {
-  return set_octree_tiling(tile_nodes, chunk_slots) ? OCT_OK : OCT_ERR_INVALID_ARG;
-}
 
 size_t oct_diag_wait_workspace_bytes(void) { return 2 * 1024 * sizeof(uint32_t); }
 

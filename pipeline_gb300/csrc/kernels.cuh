@@ -260,29 +260,6 @@ struct OctArgs {
 cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t* status,
                           cudaStream_t s, Recorder* rec = nullptr, bool tags_clear = false);
 
-// Whole-build form of stages 7-8 (octree_tiled.cu) for radix trees this
-// library built: per tile of radix nodes, its octree slots are built in
-// shared memory; writes into another tile's slot flag that slot, which a
-// fix-up kernel rebuilds afterwards (slot 0 gathers its writes in a small
-// global block). The zeroed part (root block, list count, one flag bit per
-// slot) must be zero when launch_octree_tiled starts; the list is not.
-struct OctFix {
-  unsigned long long* root_child;  // [8] (tag << 32 | value) of writes into slot 0
-  uint32_t* root_mask;             // SetChild bits of slot 0
-  uint32_t* count;                 // radix nodes in the list
-  uint32_t* flags;                 // [cap / 32 + 1] flagged slots
-  int* list;                       // [cap] radix nodes whose first slot is flagged
-  int cap;
-};
-size_t oct_fix_zero_bytes(int cap);
-size_t oct_fix_list_bytes(int cap);
-OctFix oct_fix_carve(void* zeroed, void* list, int cap);
-cudaError_t launch_octree_tiled(const OctArgs& a, const OctFix& f, uint32_t* status,
-                                cudaStream_t s, Recorder* rec = nullptr);
-// Radix nodes per tile (<= 512) and slots per shared-memory pass (<= 512) of
-// later launches; 0, 0 restores 512, 512. False for other values.
-bool set_octree_tiling(int tile_nodes, int chunk_slots);
-
 // Inclusive prefix sum of the edge counts written by launch_radix_tree_sorted
 // (which also summed them per 4,096-node tile into the scratch) that also
 // clears the octree tags of every slot stages 7-8 can touch, up to the tags'

@@ -706,7 +706,7 @@ namespace {
 
 struct LearnedBuildLayout {
   octgb::LsortPlan lp;
-  size_t misc_off, fix_off, lsort_off, keys_off, tree_off, list_off, total;
+  size_t misc_off, lsort_off, keys_off, tree_off, tags_off, total;
 };
 
 LearnedBuildLayout learned_layout(int n, int cap, int nb, int max_segments) {
@@ -714,12 +714,11 @@ LearnedBuildLayout learned_layout(int n, int cap, int nb, int max_segments) {
   LearnedBuildLayout L{};
   L.lp = lsort_plan(n, nb, max_segments);
   L.misc_off = 0;
-  L.fix_off = 256;
-  L.lsort_off = align_up(L.fix_off + oct_fix_zero_bytes(cap), 256);
+  L.lsort_off = 256;
   L.keys_off = align_up(L.lsort_off + L.lp.bytes, 256);
   L.tree_off = align_up(L.keys_off + 4 * (size_t)(n > 0 ? n : 1), 256);
-  L.list_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
-  L.total = align_up(L.list_off + oct_fix_list_bytes(cap), 256);
+  L.tags_off = align_up(L.tree_off + tree_scratch_bytes(n), 256);
+  L.total = align_up(L.tags_off + oct_tags_bytes(cap), 256);
   return L;
 }
 
@@ -818,7 +817,7 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
   int* d_unique = reinterpret_cast<int*>(w + L.misc_off + 4);
   int* d_max_slot = reinterpret_cast<int*>(w + L.misc_off + 8);
   uint32_t* keys = reinterpret_cast<uint32_t*>(w + L.keys_off);
-  cudaError_t e = cudaMemsetAsync(w, 0, L.lsort_off, s);  // misc + octree fix-up state
+  cudaError_t e = cudaMemsetAsync(w, 0, L.lsort_off, s);  // misc
   if (e == cudaSuccess)
     e = launch_lsort(reinterpret_cast<const float4*>(points), keys, n, min_coord, range,
                      static_cast<const char*>(model), L.lp, w + L.lsort_off, overflow_threshold,
@@ -828,9 +827,10 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
                                  out->tree.has_leaf_left, out->tree.has_leaf_right,
                                  out->tree.left_child, out->tree.parent, out->edge_count,
                                  w + L.tree_off, s);
+  const OctTags tags = oct_tags_carve(w + L.tags_off, out->nodes_capacity);
   if (e == cudaSuccess)
     e = launch_prefix_sum_clear_tags(n, d_unique, out->edge_count, out->prefix_sum, d_max_slot,
-                                     w + L.tree_off, status, OctTags{}, s);
+                                     w + L.tree_off, status, tags, s);
   if (e == cudaSuccess && out->nodes_capacity > 0) {
     OctArgs a{};
     a.nodes = out->nodes;
@@ -848,8 +848,7 @@ OCT_API int oct_build_octree_learned(const oct_vec4* points, int n, float min_co
     a.n_brt_host = n;
     a.d_unique = d_unique;
     a.d_max_slot = d_max_slot;
-    e = launch_octree_tiled(a, oct_fix_carve(w + L.fix_off, w + L.list_off, out->nodes_capacity),
-                            status, s, nullptr);
+    e = launch_octree(kOctMake | kOctLink | kOctFresh, a, tags, status, s, nullptr, true);
   }
   if (e == cudaSuccess) e = launch_publish_counts(d_unique, d_max_slot, status, out->d_counts, s);
   if (e == cudaSuccess && d_stats)
