@@ -544,6 +544,28 @@ def _time_events(fn, reps, stream, flush):
     return statistics.median(ts)
 
 
+def _graph_of(fn, dev):
+    """fn's launches captured once in a CUDA graph (after one eager run);
+    returns the graph's replay, or None when the launches cannot be captured."""
+    import torch
+
+    try:
+        s = torch.cuda.Stream(dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(s):
+            fn()
+        torch.cuda.current_stream(dev).wait_stream(s)
+        torch.cuda.synchronize(dev)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn()
+        torch.cuda.synchronize(dev)
+        return g.replay
+    except Exception:  # pragma: no cover - reported as null
+        torch.cuda.synchronize(dev)
+        return None
+
+
 def clustered_workload(dev, flush, reps):
     """16,777,216-point clustered cloud: learned bucketed sort vs plain."""
     import torch
@@ -640,12 +662,17 @@ def batched_workload(dev, flush, reps):
         exact &= r["oct_nodes"].tobytes() == g["oct_nodes"].tobytes()
     t_batch = _time_events(b.replay, reps, stream, flush)
     t_loop = _time_events(loop, max(2, reps // 4), stream, flush)
+    loop_graph = _graph_of(loop, dev)
+    t_loop_graph = _time_events(loop_graph, max(2, reps // 4), stream, flush) if loop_graph else None
     autotune.set_config(old_cfg)
     return {"workload": "batched_512: 512 clouds, sizes log-uniform in [1K, 1M] (seed 11), even "
                         "uniform, odd 8-Gaussian mixtures; one CUDA-graph-captured batched build",
             "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
             "per_cloud_loop_mpts": round(total / t_loop / 1e3, 1),
-            "speedup": round(t_loop / t_batch, 3), "bit_exact_spot_check": bool(exact),
+            "speedup": round(t_loop / t_batch, 3),
+            "per_cloud_loop_graph_mpts": round(total / t_loop_graph / 1e3, 1) if t_loop_graph else None,
+            "speedup_vs_graph_loop": round(t_loop_graph / t_batch, 3) if t_loop_graph else None,
+            "bit_exact_spot_check": bool(exact),
             "autotuned_sort_shape": {"radix_bits": tuned["config"][0], "warps": tuned["config"][1],
                                      "items": tuned["config"][2], "candidates_ms": tuned["all"]}}
 
@@ -716,6 +743,10 @@ def frames_workload(dev, flush, reps):
     t_batch = _time_events(b.replay, reps, stream, flush)
     t_plain = _time_events(plain_loop, max(2, reps // 4), stream, flush)
     t_learn = _time_events(learned_loop, max(2, reps // 4), stream, flush)
+    plain_graph = _graph_of(plain_loop, dev)
+    learned_graph = _graph_of(learned_loop, dev)
+    t_plain_g = _time_events(plain_graph, max(2, reps // 4), stream, flush) if plain_graph else None
+    t_learn_g = _time_events(learned_graph, max(2, reps // 4), stream, flush) if learned_graph else None
     return {"workload": "frames: 224 scan-like frames (32-255) of 122,880 points, per-frame "
                         "min/range; model fit on frames 0-31 (1024 segments, 512 buckets)",
             "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
@@ -723,6 +754,9 @@ def frames_workload(dev, flush, reps):
             "per_frame_learned_mpts": round(total / t_learn / 1e3, 1),
             "batched_vs_loop": round(t_plain / t_batch, 3),
             "learned_vs_plain_per_frame": round(t_plain / t_learn, 3),
+            "per_frame_plain_graph_mpts": round(total / t_plain_g / 1e3, 1) if t_plain_g else None,
+            "per_frame_learned_graph_mpts": round(total / t_learn_g / 1e3, 1) if t_learn_g else None,
+            "batched_vs_graph_loop": round(t_plain_g / t_batch, 3) if t_plain_g else None,
             "bit_exact_spot_check": bool(exact), "learned_fallbacks_in_spot_check": int(fallbacks),
             "overflow_frac_max": round(max(overflow), 5), "fit_loss": model.header()["loss"]}
 
@@ -796,8 +830,8 @@ def sort_bar_workload(dev, flush, reps, pts):
     return out
 
 
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_uniform_4m.txt")
-TRAFFIC_POINTS = 4194304
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_uniform_16m.txt")
+TRAFFIC_POINTS = 16777216
 TRAFFIC_KERNELS = {"morton+histogram": ["morton_kernel<10, 1>"],
                    "unique": ["unique_count_kernel", "unique_deltas_kernel"],
                    "radix tree+edge count": ["tree_nodes_kernel"],
@@ -808,10 +842,10 @@ TRAFFIC_KERNELS = {"morton+histogram": ["morton_kernel<10, 1>"],
 
 def read_traffic(kernel_step: str, n: int):
     """DRAM bytes (read + write) of one build step (the sum over its kernels)
-    from the committed ncu summary of the 4,194,304-point build, scaled to n
-    points; None when the summary does not cover every kernel of the step. At
-    that size outputs may still sit in L2 when a kernel ends, so this can fall
-    below the algorithmic bytes."""
+    from the committed ncu summary of a 16,777,216-point build (one launch of
+    each kernel, measured at that size), scaled by n / 16,777,216 when the
+    bench runs another size; None when the summary does not cover every
+    kernel of the step."""
     names = TRAFFIC_KERNELS.get(kernel_step)
     if not names or not os.path.exists(TRAFFIC_FILE):
         return None
@@ -820,9 +854,9 @@ def read_traffic(kernel_step: str, n: int):
         for ln in f:
             parts = ln.split()
             for name in names:
-                if name not in found and len(parts) >= 4 and ln.strip().startswith(name):
+                if name not in found and len(parts) >= 5 and ln.strip().startswith(name):
                     try:
-                        found[name] = float(parts[-3]) + float(parts[-2])
+                        found[name] = float(parts[-4]) + float(parts[-3])
                     except ValueError:
                         pass
     if len(found) != len(names):
