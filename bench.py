@@ -740,7 +740,23 @@ def frames_workload(dev, flush, reps):
         overflow.append(st["overflow_frac"])
         exact &= r["oct_nodes"].tobytes() == b.cloud_result(c, counts)["oct_nodes"].tobytes()
         exact &= r["oct_nodes"].tobytes() == lr_["oct_nodes"].tobytes()
+    # learned + batched: one model (64 buckets per frame) fit on frames 0-31
+    # drives the batched build's sort for frames 32-255
+    nb_lb = 64
+    t0 = time.perf_counter()
+    model_lb = LearnedCDF(max_segments=1024).fit(sample, n_segments=1024, steps=100, lr=0.05,
+                                                 n_buckets=nb_lb)
+    torch.cuda.synchronize(dev)
+    fit_lb_ms = (time.perf_counter() - t0) * 1e3
+    lbb = BatchOctreeBuilder(sizes, device=dev, model=model_lb, n_buckets=nb_lb)
+    lbb.capture(pts, d_min, d_rg)
+    lbb.replay()
+    torch.cuda.synchronize(dev)
+    lb_stats = lbb.learned_stats()
+    lb_exact = (torch.equal(lbb.counts, b.counts) and torch.equal(lbb.codes, b.codes)
+                and torch.equal(lbb.nodes, b.nodes))
     t_batch = _time_events(b.replay, reps, stream, flush)
+    t_lbatch = _time_events(lbb.replay, reps, stream, flush)
     t_plain = _time_events(plain_loop, max(2, reps // 4), stream, flush)
     t_learn = _time_events(learned_loop, max(2, reps // 4), stream, flush)
     plain_graph = _graph_of(plain_loop, dev)
@@ -757,6 +773,14 @@ def frames_workload(dev, flush, reps):
             "per_frame_plain_graph_mpts": round(total / t_plain_g / 1e3, 1) if t_plain_g else None,
             "per_frame_learned_graph_mpts": round(total / t_learn_g / 1e3, 1) if t_learn_g else None,
             "batched_vs_graph_loop": round(t_plain_g / t_batch, 3) if t_plain_g else None,
+            "learned_batched_mpts": round(total / t_lbatch / 1e3, 1),
+            "learned_batched_vs_batched": round(t_batch / t_lbatch, 3),
+            "learned_batched_vs_graph_loop": round(t_plain_g / t_lbatch, 3) if t_plain_g else None,
+            "learned_batched_vs_stream_loop": round(t_plain / t_lbatch, 3),
+            "learned_batched_bit_exact_vs_batched": bool(lb_exact),
+            "learned_batched_fallback": lb_stats["fallback"],
+            "learned_batched_max_bucket": lb_stats["max_bucket"],
+            "learned_batched_fit_ms": round(fit_lb_ms, 2),
             "bit_exact_spot_check": bool(exact), "learned_fallbacks_in_spot_check": int(fallbacks),
             "overflow_frac_max": round(max(overflow), 5), "fit_loss": model.header()["loss"]}
 
@@ -864,6 +888,69 @@ def read_traffic(kernel_step: str, n: int):
     return int(sum(found.values()) * 1e6 * n / TRAFFIC_POINTS)
 
 
+def run_sharded_batched(args, rank, world, local_rank):
+    """--shard batched: the 512-cloud batch split over the ranks by
+    shard_clouds (greedy longest-first on point counts, no collective on the
+    data path); each rank builds its clouds in one graph-replayed batched build.
+    value = all ranks' points / the slowest rank's time per step."""
+    import torch
+    import torch.distributed as dist
+
+    from pipeline_gb300 import datasets
+    from pipeline_gb300.batch import BatchOctreeBuilder, shard_clouds
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    clouds = datasets.batched(512, seed=11)
+    sizes = [len(c) for c in clouds]
+    mine = shard_clouds(sizes, world)[rank]
+    pts = torch.from_numpy(np.concatenate([clouds[c] for c in mine], 0)).to(dev)
+    mins = torch.zeros(len(mine), dtype=torch.float32, device=dev)
+    ranges = torch.full((len(mine),), RANGE, dtype=torch.float32, device=dev)
+    b = BatchOctreeBuilder([sizes[c] for c in mine], device=dev)
+    b.capture(pts, mins, ranges)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 3)):
+        b.replay()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        b.replay()
+        ends[k].record(stream)
+    barrier()
+    ms = statistics.mean(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    st = b.cloud_counts()[:, 3]
+    if int(np.bitwise_or.reduce(st.astype(np.int64))) != 0:
+        raise RuntimeError("device status set")
+    total = int(sum(sizes))
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Mpoints/s octree build, batched 512 clouds sharded over ranks",
+            "value": round(total / ms / 1e3, 1), "unit": "Mpoints/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic",
+            "config": {"workload": "batched_512 sharded: 512 clouds, sizes log-uniform in [1K, 1M] "
+                                   "(seed 11), split over ranks longest-first, no collective",
+                       "clouds_rank0": len(mine), "points_rank0": int(sum(sizes[c] for c in mine)),
+                       "l2": "flushed between steps (256 MiB write)"}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -876,6 +963,8 @@ def main():
     ap.add_argument("--profile-only", nargs="?", const="plain",
                     choices=["plain", "learned", "batched"],
                     help="warm-up builds plus one build, no timing or output (for ncu captures)")
+    ap.add_argument("--shard", choices=["batched"], default=None,
+                    help="split the 512-cloud batched workload over the ranks (one line)")
     ap.add_argument("--points", type=int, default=N_POINTS,
                     help="cloud size for --profile-only (smaller cases for multi-pass ncu captures)")
     args = ap.parse_args()
@@ -891,6 +980,8 @@ def main():
 
         dist.init_process_group("nccl")
     try:
+        if args.shard == "batched":
+            return run_sharded_batched(args, rank, world, local_rank)
         return run_ours(args, rank, world, local_rank)
     finally:
         if world > 1:

@@ -395,6 +395,24 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* plan, const void* d_tab
                                    int32_t* d_cloud_counts, void* workspace,
                                    size_t workspace_bytes, oct_stream_t stream);
 
+/* Learned + batched build (no counterpart in the reference): the batched
+ * build with stage 2 done by one learned CDF model shared by the clouds
+ * (fit on their own per-cloud Morton codes, oct_lcdf_fit): per cloud, each
+ * key goes to one of n_buckets buckets, each bucket is sorted in shared
+ * memory. When a bucket holds more than 8,192 keys the plain LSD passes sort
+ * the batch instead (decided on the device). Outputs are the batched build's,
+ * bit for bit. d_stats (may be NULL): {1 if the LSD passes ran, largest
+ * bucket}. Workspace: oct_batch_learned_workspace_bytes(plan, n_buckets).
+ * Needs a sort shape with an odd pass count (the default: 3 x 10 bits). */
+OCT_API size_t oct_batch_learned_workspace_bytes(const oct_batch_plan* plan, int n_buckets);
+OCT_API int oct_build_octree_batch_learned(const oct_batch_plan* plan, const void* d_tables,
+                                           const oct_vec4* points, const float* d_mins,
+                                           const float* d_ranges, const void* model,
+                                           int max_segments, int n_buckets,
+                                           const oct_build_outputs* out, int32_t* d_cloud_counts,
+                                           uint32_t* d_stats, void* workspace,
+                                           size_t workspace_bytes, oct_stream_t stream);
+
 /* Synchronous convenience: copies d_counts to the host after the stream
  * drains and maps the status word to OCT_ERR_DEVICE / OCT_ERR_CAPACITY. */
 OCT_API int oct_read_counts(const int32_t* d_counts, int32_t* h_counts, oct_stream_t stream);

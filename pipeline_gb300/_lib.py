@@ -123,6 +123,9 @@ SIGNATURES = {
     "oct_batch_plan_info": (I, [P, P]),
     "oct_batch_upload_tables": (I, [P, P, P]),
     "oct_build_octree_batch": (I, [P, P, P, P, P, C.POINTER(OctBuildOutputs), P, P, Z, P]),
+    "oct_batch_learned_workspace_bytes": (Z, [P, I]),
+    "oct_build_octree_batch_learned": (I, [P, P, P, P, P, P, I, I, C.POINTER(OctBuildOutputs), P,
+                                           P, P, Z, P]),
     "oct_build_sort_form": (I, [P, I, I, P]),
     "oct_build_step_count": (I, []),
     "oct_build_step_name": (C.c_char_p, [I]),

@@ -32,7 +32,11 @@ def shard_clouds(sizes, world: int) -> list[list[int]]:
 
 
 class BatchOctreeBuilder:
-    def __init__(self, sizes, node_caps=None, device="cuda"):
+    """Batched build of clouds of the given sizes. With `model` (a fitted
+    LearnedCDF shared by the clouds) stage 2 is the learned bucket sort with
+    `n_buckets` buckets per cloud (oct_build_octree_batch_learned)."""
+
+    def __init__(self, sizes, node_caps=None, device="cuda", model=None, n_buckets=None):
         self.lib = _lib.load()
         self.device = torch.device(device)
         self.sizes = np.asarray(sizes, np.int32)
@@ -49,6 +53,13 @@ class BatchOctreeBuilder:
         self.node_start = np.concatenate([[0], np.cumsum(cap_arr.astype(np.int64))]).astype(np.int64)
         dev = self.device
         n = max(self.n, 1)
+        self.model = model
+        self.nb = int(n_buckets or (model.n_buckets if model is not None else 0))
+        if model is not None:
+            wbytes = self.lib.oct_batch_learned_workspace_bytes(self.plan, self.nb)
+            if not wbytes:
+                raise ValueError("bad bucket count for the learned batched build")
+        self.stats = torch.zeros(2, dtype=torch.int32, device=dev)
         self.tables = torch.empty(max(tbytes, 256), dtype=torch.uint8, device=dev)
         self.workspace = torch.empty(max(wbytes, 256), dtype=torch.uint8, device=dev)
         self.codes = torch.empty(n, dtype=torch.int32, device=dev)
@@ -85,12 +96,27 @@ class BatchOctreeBuilder:
         if points.numel() < 4 * self.n or not points.is_cuda or points.dtype != torch.float32:
             raise ValueError("points: float32 CUDA tensor of the batch's total size x 4")
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if self.model is not None:
+            rc = self.lib.oct_build_octree_batch_learned(
+                self.plan, C.c_void_p(self.tables.data_ptr()), C.c_void_p(points.data_ptr()),
+                C.c_void_p(mins.data_ptr()), C.c_void_p(ranges.data_ptr()),
+                C.c_void_p(self.model.blob.data_ptr()), self.model.max_segments, self.nb,
+                C.byref(self._out), C.c_void_p(self.counts.data_ptr()),
+                C.c_void_p(self.stats.data_ptr()), C.c_void_p(self.workspace.data_ptr()),
+                self.workspace.numel(), C.c_void_p(s.cuda_stream))
+            _lib.check(rc, "oct_build_octree_batch_learned")
+            return
         rc = self.lib.oct_build_octree_batch(
             self.plan, C.c_void_p(self.tables.data_ptr()), C.c_void_p(points.data_ptr()),
             C.c_void_p(mins.data_ptr()), C.c_void_p(ranges.data_ptr()), C.byref(self._out),
             C.c_void_p(self.counts.data_ptr()), C.c_void_p(self.workspace.data_ptr()),
             self.workspace.numel(), C.c_void_p(s.cuda_stream))
         _lib.check(rc, "oct_build_octree_batch")
+
+    def learned_stats(self) -> dict:
+        """{fallback: 1 if the LSD passes sorted the batch, max_bucket}."""
+        v = self.stats.cpu().tolist()
+        return {"fallback": int(v[0]), "max_bucket": int(v[1])}
 
     def capture(self, points, mins, ranges):
         g = torch.cuda.CUDAGraph()

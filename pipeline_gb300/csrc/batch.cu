@@ -34,6 +34,7 @@
 #include <new>
 #include <vector>
 
+#include "lsort.cuh"
 #include "octree.cuh"
 #include "tree.cuh"
 
@@ -166,7 +167,8 @@ __global__ void __launch_bounds__(1024)
 constexpr int kTsGroups = 8;
 __global__ void __launch_bounds__(32 * kTsGroups)
     batch_tile_scan_kernel(uint32_t* __restrict__ th, int bins, const uint32_t* __restrict__ base,
-                           int passes, int pass, BatchDev B) {
+                           int passes, int pass, BatchDev B, const uint32_t* __restrict__ gate) {
+  if (gate && *gate == 0) return;
   __shared__ uint32_t part[kTsGroups][33];
   const int c = blockIdx.x;
   const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
@@ -580,11 +582,25 @@ OCT_API int oct_batch_upload_tables(const oct_batch_plan* P, void* d_tables, oct
   return e == cudaSuccess ? OCT_OK : batch_fail(e, "oct_batch_upload_tables");
 }
 
-OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables,
-                                   const oct_vec4* points, const float* d_mins,
-                                   const float* d_ranges, const oct_build_outputs* out,
-                                   int32_t* d_cloud_counts, void* workspace,
-                                   size_t workspace_bytes, oct_stream_t stream) {
+}  // extern "C"
+
+namespace {
+
+// The learned stage-2 sort of a batched build (nullptr: the LSD passes).
+struct BatchLearned {
+  const char* model;
+  octgb::LcdfLayout L;
+  int nb;
+  char* ws;            // lbatch_flag_bytes() zeroed per build, then the scratch
+  uint32_t* d_stats;   // optional: {fallback, largest bucket}
+};
+
+size_t lbatch_flag_bytes() { return 256; }
+
+int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* points,
+                const float* d_mins, const float* d_ranges, const oct_build_outputs* out,
+                int32_t* d_cloud_counts, void* workspace, size_t workspace_bytes,
+                oct_stream_t stream, const BatchLearned* lb) {
   using namespace octgb;
   if (!P || !d_tables || !d_mins || !d_ranges || !out || !d_cloud_counts || !workspace ||
       (reinterpret_cast<uintptr_t>(workspace) & 255))
@@ -611,6 +627,12 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
   const int sms = device_sm_count();
   cudaError_t e = cudaMemsetAsync(w, 0, P->zero_bytes, s);
   if (e != cudaSuccess) return batch_fail(e, "batch: clear");
+  uint32_t* fallback = nullptr;
+  if (lb) {
+    e = cudaMemsetAsync(lb->ws, 0, lbatch_flag_bytes(), s);
+    if (e != cudaSuccess) return batch_fail(e, "batch: clear learned flags");
+    fallback = reinterpret_cast<uint32_t*>(lb->ws);
+  }
   if (P->N > 0) {
     const int mgrid = std::max(1, std::min(B.Ts, sms * 16));
     const size_t msm = 4 * (size_t)passes * bins;
@@ -623,21 +645,45 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
                                                      B, hist, passes, status);
       batch_hist_scan_kernel<8><<<P->C * passes, 256, 0, s>>>(hist, base, B, passes);
     }
+    // the sorted keys land in the buffer the LSD passes end in
+    uint32_t* sorted = (passes & 1) ? kb : ka;
+    if (lb) {
+      LbatchArgs la{};
+      la.keys = ka;
+      la.out = sorted;
+      la.tiles = B.sort_tiles;
+      la.n_tiles = B.Ts;
+      la.start = B.start;
+      la.cloud_tile0 = B.cloud_tile0;
+      la.C = P->C;
+      la.blob = lb->model;
+      la.L = lb->L;
+      la.nb = lb->nb;
+      la.scratch = lb->ws + lbatch_flag_bytes();
+      la.fallback = fallback;
+      la.max_bucket = fallback + 1;
+      e = launch_lbatch_sort(la, s);
+      if (e != cudaSuccess) return batch_fail(e, "batch: learned sort");
+      // When the learned sort keeps the result, `sorted` must not be the
+      // passes' input: with an even pass count it is ka itself, so the
+      // learned path is only offered for odd pass counts (host check).
+    }
     uint32_t* a = ka;
     uint32_t* b = kb;
     for (int p = 0; p < passes && e == cudaSuccess; ++p) {
       const int shift = p * rb;
-      e = launch_tile_hist(rb, a, P->N, shift, B.sort_tiles, B.Ts, th, s);
+      e = launch_tile_hist(rb, a, P->N, shift, B.sort_tiles, B.Ts, th, s, fallback);
       if (e != cudaSuccess) break;
       batch_tile_scan_kernel<<<dim3(P->C, (bins + 31) / 32), 32 * kTsGroups, 0, s>>>(
-          th, bins, base, passes, p, B);
-      e = launch_pass(sp, p > 0, a, b, shift, nullptr, nullptr, nullptr, th, status, nullptr, s,
+          th, bins, base, passes, p, B, fallback);
+      e = launch_pass(sp, p > 0, a, b, shift, nullptr, nullptr, nullptr, th, status, fallback, s,
                       B.sort_tiles, B.Ts);
       uint32_t* t = a;
       a = b;
       b = t;
     }
     if (e != cudaSuccess) return batch_fail(e, "batch: sort");
+    a = sorted;
     void* tree_ws = w + P->w_tree;
     const TreeScratch TS = tree_scratch_carve_tiles(tree_ws, B.T4);
     e = launch_batch_unique_deltas(a, B.tiles4k, B.T4, B.start, out->codes, unique_c, tree_ws, s);
@@ -670,8 +716,53 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
   } else {
     e = cudaMemsetAsync(d_cloud_counts, 0, 16 * (size_t)P->C, s);
   }
+  if (e == cudaSuccess && lb && lb->d_stats)
+    e = cudaMemcpyAsync(lb->d_stats, lb->ws, 2 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e == cudaSuccess ? OCT_OK : batch_fail(e, "oct_build_octree_batch");
+}
+
+}  // namespace
+
+extern "C" {
+
+OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables,
+                                   const oct_vec4* points, const float* d_mins,
+                                   const float* d_ranges, const oct_build_outputs* out,
+                                   int32_t* d_cloud_counts, void* workspace,
+                                   size_t workspace_bytes, oct_stream_t stream) {
+  return batch_build(P, d_tables, points, d_mins, d_ranges, out, d_cloud_counts, workspace,
+                     workspace_bytes, stream, nullptr);
+}
+
+OCT_API size_t oct_batch_learned_workspace_bytes(const oct_batch_plan* P, int n_buckets) {
+  if (!P || n_buckets < 1 || n_buckets > 65536) return 0;
+  return octgb::align_up(P->ws_bytes, 256) + lbatch_flag_bytes() +
+         octgb::lbatch_scratch_bytes((int)P->sort_tiles.size(), P->C, n_buckets);
+}
+
+OCT_API int oct_build_octree_batch_learned(const oct_batch_plan* P, const void* d_tables,
+                                           const oct_vec4* points, const float* d_mins,
+                                           const float* d_ranges, const void* model,
+                                           int max_segments, int n_buckets,
+                                           const oct_build_outputs* out, int32_t* d_cloud_counts,
+                                           uint32_t* d_stats, void* workspace,
+                                           size_t workspace_bytes, oct_stream_t stream) {
+  using namespace octgb;
+  if (!P || !model || max_segments < 1 || max_segments > kLcdfMaxSegments || n_buckets < 1 ||
+      n_buckets > 65536 || lsort_hist_smem(n_buckets, max_segments) > (size_t)kLsortMaxSmem)
+    return OCT_ERR_INVALID_ARG;
+  if ((P->sp.passes & 1) == 0) return OCT_ERR_INVALID_ARG;  // see batch_build
+  if (!workspace || workspace_bytes < oct_batch_learned_workspace_bytes(P, n_buckets))
+    return workspace ? OCT_ERR_WORKSPACE : OCT_ERR_INVALID_ARG;
+  BatchLearned lb;
+  lb.model = static_cast<const char*>(model);
+  lb.L = lcdf_layout(max_segments);
+  lb.nb = n_buckets;
+  lb.ws = static_cast<char*>(workspace) + align_up(P->ws_bytes, 256);
+  lb.d_stats = d_stats;
+  return batch_build(P, d_tables, points, d_mins, d_ranges, out, d_cloud_counts, workspace,
+                     workspace_bytes, stream, &lb);
 }
 
 }  // extern "C"

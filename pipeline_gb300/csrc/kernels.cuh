@@ -93,7 +93,8 @@ cudaError_t launch_pass(const SortPlan& p, bool stable, const uint32_t* src, uin
                         const uint32_t* tile_prefix, uint32_t* status, const uint32_t* gate,
                         cudaStream_t s, const int4* tdesc, int tiles, DigitAlt alt = DigitAlt{});
 cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
-                             const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s);
+                             const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s,
+                             const uint32_t* gate = nullptr);
 void set_sort_config(const SortConfig& c);
 SortConfig get_sort_config();
 

@@ -593,6 +593,171 @@ __global__ void __launch_bounds__(256)
   for (int i = threadIdx.x; i < c; i += 256) dst[i] = src[i];
 }
 
+// ----------------------------------------------------- batched learned sort --
+// The clouds of a batch share one model over their own (per-cloud
+// quantised) Morton codes. Bucket b of cloud c holds the cloud's keys with
+// bucket(key) == b, so each cloud's keys sorted bucket by bucket are the
+// cloud's sorted keys; duplicates are kept (the batched unique that follows
+// removes them).
+//   lb_hist     per sort tile (tiles never cross clouds): bucket counts
+//   lb_scan     per cloud: every tile's offset in every bucket, bucket starts
+//               and sizes; a bucket above kBkCache keys sets `fallback`
+//   lb_scatter  per tile: each key to its bucket (any order inside it)
+//   lb_bucket   one CTA per (cloud, bucket): the stable shared-memory radix
+//               sort of the bucket's keys (bucket_radix_sort), in place
+// With `fallback` set, lb_scatter and lb_bucket return at once and the plain
+// LSD passes (gated on the same flag) sort the batch instead.
+__global__ void __launch_bounds__(256)
+    lb_hist_kernel(const uint32_t* __restrict__ keys, const int4* __restrict__ tiles,
+                   const char* __restrict__ blob, LcdfLayout L, int nb,
+                   uint32_t* __restrict__ tile_off) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  uint32_t* s_hist = reinterpret_cast<uint32_t*>(sm);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0;
+  const BucketLookup q = load_lookup(blob, L, nb, s_hist + nb,
+                                     reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
+  const int4 d = tiles[blockIdx.x];
+  for (int i = d.x + (int)threadIdx.x; i < d.y; i += blockDim.x)
+    atomicAdd(&s_hist[bucket_of(q, keys[i])], 1u);
+  __syncthreads();
+  uint32_t* row = tile_off + (size_t)blockIdx.x * nb;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) row[b] = s_hist[b];
+}
+
+__global__ void __launch_bounds__(1024)
+    lb_scan_kernel(const int* __restrict__ start, const int* __restrict__ cloud_tile0, int nb,
+                   uint32_t* __restrict__ tile_off, uint32_t* __restrict__ bstart,
+                   uint32_t* __restrict__ bcount, uint32_t* __restrict__ fallback,
+                   uint32_t* __restrict__ max_bucket) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  extern __shared__ __align__(16) unsigned char sm[];
+  uint32_t* tot = reinterpret_cast<uint32_t*>(sm);
+  const int c = blockIdx.x;
+  const int t0 = cloud_tile0[c], t1 = cloud_tile0[c + 1];
+  // per bucket: offsets of the cloud's tiles inside the bucket (column scan)
+  uint32_t big = 0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    uint32_t run = 0;
+    for (int t = t0; t < t1; ++t) {
+      const uint32_t v = tile_off[(size_t)t * nb + b];
+      tile_off[(size_t)t * nb + b] = run;
+      run += v;
+    }
+    tot[b] = run;
+    big = max(big, run);
+  }
+  __syncthreads();
+  // bucket starts: exclusive scan of the totals (each thread a run of buckets)
+  const int per = (nb + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  uint32_t sum = 0;
+  for (int b = b0; b < min(b0 + per, nb); ++b) sum += tot[b];
+  uint32_t run = block_exclusive_sum<1024>(sum, s_warp, &s_total) + (uint32_t)start[c];
+  for (int b = b0; b < min(b0 + per, nb); ++b) {
+    bstart[(size_t)c * nb + b] = run;
+    bcount[(size_t)c * nb + b] = tot[b];
+    tot[b] = run;
+    run += bcount[(size_t)c * nb + b];
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int t = t0; t < t1; ++t) tile_off[(size_t)t * nb + b] += tot[b];
+  big = __reduce_max_sync(0xffffffffu, big);
+  if ((threadIdx.x & 31) == 0 && big) {
+    atomicMax(max_bucket, big);
+    if (big > (uint32_t)kBkCache) atomicOr(fallback, 1u);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    lb_scatter_kernel(const uint32_t* __restrict__ keys, uint32_t* __restrict__ out,
+                      const int4* __restrict__ tiles, const char* __restrict__ blob, LcdfLayout L,
+                      int nb, const uint32_t* __restrict__ tile_off,
+                      const uint32_t* __restrict__ fallback) {
+  if (*fallback) return;
+  extern __shared__ __align__(16) unsigned char sm[];
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
+  const uint32_t* row = tile_off + (size_t)blockIdx.x * nb;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) cursor[b] = row[b];
+  const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
+                                     reinterpret_cast<uint16_t*>(cursor + 2 * nb));
+  const int4 d = tiles[blockIdx.x];
+  for (int i = d.x + (int)threadIdx.x; i < d.y; i += blockDim.x) {
+    const uint32_t k = keys[i];
+    out[atomicAdd(&cursor[bucket_of(q, k)], 1u)] = k;
+  }
+}
+
+__global__ void __launch_bounds__(kBkThreads, 3)
+    lb_bucket_kernel(uint32_t* __restrict__ keys, const uint32_t* __restrict__ bstart,
+                     const uint32_t* __restrict__ bcount, const uint32_t* __restrict__ fallback) {
+  if (*fallback) return;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  BucketSmem& S = *reinterpret_cast<BucketSmem*>(sm_raw);
+  const int cnt = (int)bcount[blockIdx.x];
+  if (cnt <= 1) return;
+  uint32_t* g = keys + bstart[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  uint32_t kmin = 0xffffffffu, kmax = 0;
+  for (int i = tid; i < cnt; i += kBkThreads) {
+    const uint32_t k = g[i];
+    S.buf[i] = k;
+    kmin = min(kmin, k);
+    kmax = max(kmax, k);
+  }
+  kmin = __reduce_min_sync(0xffffffffu, kmin);
+  kmax = __reduce_max_sync(0xffffffffu, kmax);
+  if (lane == 0) {
+    S.red[0][wid] = kmin;
+    S.red[1][wid] = kmax;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t a = lane < kBkWarps ? S.red[0][lane] : 0xffffffffu;
+    uint32_t z = lane < kBkWarps ? S.red[1][lane] : 0u;
+    a = __reduce_min_sync(0xffffffffu, a);
+    z = __reduce_max_sync(0xffffffffu, z);
+    if (lane == 0) {
+      S.misc[1] = a;
+      S.misc[2] = z;
+    }
+  }
+  __syncthreads();
+  kmin = S.misc[1];
+  kmax = S.misc[2];
+  if (kmin == kmax) return;  // all keys equal: already sorted
+  const int bits = 32 - __clz(kmax - kmin);
+  const uint32_t* sorted = bucket_radix_sort(S.buf, S.buf + kBkCache, cnt, kmin, bits, S);
+  for (int i = tid; i < cnt; i += kBkThreads) g[i] = sorted[i];
+}
+
+size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb) {
+  return align_up(4 * (size_t)n_tiles * nb, 256) + 2 * align_up(4 * (size_t)n_clouds * nb, 256);
+}
+
+cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  char* w = static_cast<char*>(a.scratch);
+  uint32_t* tile_off = reinterpret_cast<uint32_t*>(w);
+  uint32_t* bstart = reinterpret_cast<uint32_t*>(w + align_up(4 * (size_t)a.n_tiles * a.nb, 256));
+  uint32_t* bcount = bstart + align_up(4 * (size_t)a.C * a.nb, 256) / 4;
+  const size_t hsm = lsort_hist_smem(a.nb, a.L.max_knots);
+  if (hsm > (size_t)kLsortMaxSmem) return cudaErrorInvalidValue;
+  cudaError_t e = set_smem_limit(lb_hist_kernel, (int)hsm);
+  if (e == cudaSuccess) e = set_smem_limit(lb_scatter_kernel, (int)hsm);
+  if (e == cudaSuccess) e = set_smem_limit(lb_bucket_kernel, (int)sizeof(BucketSmem));
+  if (e != cudaSuccess) return e;
+  lb_hist_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, a.tiles, a.blob, a.L, a.nb, tile_off);
+  lb_scan_kernel<<<a.C, 1024, 4 * (size_t)a.nb, s>>>(a.start, a.cloud_tile0, a.nb, tile_off,
+                                                     bstart, bcount, a.fallback, a.max_bucket);
+  lb_scatter_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, a.out, a.tiles, a.blob, a.L, a.nb,
+                                                tile_off, a.fallback);
+  lb_bucket_kernel<<<a.C * a.nb, kBkThreads, sizeof(BucketSmem), s>>>(a.out, bstart, bcount,
+                                                                      a.fallback);
+  return cudaGetLastError();
+}
+
 // Gate for the fallback launches: 1 when the learned path gave up.
 __global__ void lsort_gate_kernel(const LsortStats* stats, uint32_t* gate) {
   *gate = stats->fallback ? 1u : 0u;

@@ -41,4 +41,26 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
                          uint32_t* out, int* d_unique, uint32_t* status, cudaStream_t s,
                          Recorder* rec);
 
+// Learned bucket sort of a batch of clouds (keys keep their duplicates):
+// each cloud's keys sorted, in `out`, unless a bucket exceeds the shared-memory
+// sort's capacity, which sets *fallback (zeroed by the caller) and leaves
+// `out` to a sort gated on that flag.
+struct LbatchArgs {
+  const uint32_t* keys;      // cloud-concatenated Morton codes
+  uint32_t* out;             // cloud-concatenated sorted codes
+  const int4* tiles;         // sort tiles {lo, hi, cloud, the cloud's first tile}
+  int n_tiles;
+  const int* start;          // [C + 1] cloud starts
+  const int* cloud_tile0;    // [C + 1] first tile of each cloud
+  int C;
+  const char* blob;          // the model
+  LcdfLayout L;
+  int nb;                    // buckets per cloud
+  void* scratch;             // lbatch_scratch_bytes(n_tiles, C, nb), not zeroed
+  uint32_t* fallback;        // zeroed before the call
+  uint32_t* max_bucket;      // zeroed before the call
+};
+size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb);
+cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s);
+
 }  // namespace octgb

@@ -797,13 +797,16 @@ bool msd_plan_ok(const SortPlan& p) {
 }
 
 cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int shift,
-                             const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s) {
+                             const int4* tdesc, int tiles, uint32_t* th, cudaStream_t s,
+                             const uint32_t* gate) {
+  // a gated launch walks the tiles from a capped grid (few no-op CTAs)
+  const int grid = gate ? tile_hist_grid(tiles) : tiles;
   if (radix_bits == 10)
-    tile_hist_kernel<10><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc, nullptr,
-                                               tiles, DigitAlt{});
+    tile_hist_kernel<10><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles,
+                                              DigitAlt{});
   else
-    tile_hist_kernel<8><<<tiles, 256, 0, s>>>(keys, n, shift, 0, th, nullptr, tdesc, nullptr,
-                                              tiles, DigitAlt{});
+    tile_hist_kernel<8><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles,
+                                             DigitAlt{});
   return cudaGetLastError();
 }
 
