@@ -399,10 +399,13 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* plan, const void* d_tab
  * build with stage 2 done by one learned CDF model shared by the clouds
  * (fit on their own per-cloud Morton codes, oct_lcdf_fit): per cloud, each
  * key goes to one of n_buckets buckets, each bucket is sorted in shared
- * memory. When a bucket holds more than 8,192 keys the plain LSD passes sort
- * the batch instead (decided on the device). Outputs are the batched build's,
- * bit for bit. d_stats (may be NULL): {1 if the LSD passes ran, largest
- * bucket}. Workspace: oct_batch_learned_workspace_bytes(plan, n_buckets).
+ * memory down to its unique keys (a bitmap over the bucket's key span, or a
+ * radix or bitonic sort). When a bucket fits none of those forms the plain
+ * LSD passes sort the batch instead (decided on the device). Outputs are the
+ * batched build's, bit for bit. d_stats (may be NULL): 12 words, as
+ * oct_build_octree_learned's (word 0: 1 if the LSD passes ran; word 3: the
+ * largest bucket; words 7-9: buckets done by bitmap, radix and bitonic sort).
+ * Workspace: oct_batch_learned_workspace_bytes(plan, n_buckets).
  * Needs a sort shape with an odd pass count (the default: 3 x 10 bits). */
 OCT_API size_t oct_batch_learned_workspace_bytes(const oct_batch_plan* plan, int n_buckets);
 OCT_API int oct_build_octree_batch_learned(const oct_batch_plan* plan, const void* d_tables,

@@ -59,7 +59,7 @@ class BatchOctreeBuilder:
             wbytes = self.lib.oct_batch_learned_workspace_bytes(self.plan, self.nb)
             if not wbytes:
                 raise ValueError("bad bucket count for the learned batched build")
-        self.stats = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.stats = torch.zeros(12, dtype=torch.int32, device=dev)  # LsortStats
         self.tables = torch.empty(max(tbytes, 256), dtype=torch.uint8, device=dev)
         self.workspace = torch.empty(max(wbytes, 256), dtype=torch.uint8, device=dev)
         self.codes = torch.empty(n, dtype=torch.int32, device=dev)
@@ -114,9 +114,11 @@ class BatchOctreeBuilder:
         _lib.check(rc, "oct_build_octree_batch")
 
     def learned_stats(self) -> dict:
-        """{fallback: 1 if the LSD passes sorted the batch, max_bucket}."""
+        """Learned stage of the last build: fallback (1 if the LSD passes
+        sorted the batch), the largest bucket, buckets per bucket form."""
         v = self.stats.cpu().tolist()
-        return {"fallback": int(v[0]), "max_bucket": int(v[1])}
+        return {"fallback": int(v[0]), "max_bucket": int(v[3]), "bitmap_buckets": int(v[7]),
+                "radix_buckets": int(v[8]), "bitonic_buckets": int(v[9])}
 
     def capture(self, points, mins, ranges):
         g = torch.cuda.CUDAGraph()

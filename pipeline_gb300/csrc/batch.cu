@@ -592,7 +592,7 @@ struct BatchLearned {
   octgb::LcdfLayout L;
   int nb;
   char* ws;            // lbatch_flag_bytes() zeroed per build, then the scratch
-  uint32_t* d_stats;   // optional: {fallback, largest bucket}
+  uint32_t* d_stats;   // optional: LsortStats (12 words)
 };
 
 size_t lbatch_flag_bytes() { return 256; }
@@ -627,11 +627,11 @@ int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* p
   const int sms = device_sm_count();
   cudaError_t e = cudaMemsetAsync(w, 0, P->zero_bytes, s);
   if (e != cudaSuccess) return batch_fail(e, "batch: clear");
-  uint32_t* fallback = nullptr;
+  uint32_t* fallback = nullptr;  // gate of the LSD passes: LsortStats::fallback
   if (lb) {
     e = cudaMemsetAsync(lb->ws, 0, lbatch_flag_bytes(), s);
     if (e != cudaSuccess) return batch_fail(e, "batch: clear learned flags");
-    fallback = reinterpret_cast<uint32_t*>(lb->ws);
+    fallback = &reinterpret_cast<LsortStats*>(lb->ws)->fallback;
   }
   if (P->N > 0) {
     const int mgrid = std::max(1, std::min(B.Ts, sms * 16));
@@ -656,17 +656,17 @@ int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* p
       la.start = B.start;
       la.cloud_tile0 = B.cloud_tile0;
       la.C = P->C;
+      la.n = P->N;
       la.blob = lb->model;
       la.L = lb->L;
       la.nb = lb->nb;
       la.scratch = lb->ws + lbatch_flag_bytes();
-      la.fallback = fallback;
-      la.max_bucket = fallback + 1;
+      la.stats = reinterpret_cast<LsortStats*>(lb->ws);
       e = launch_lbatch_sort(la, s);
       if (e != cudaSuccess) return batch_fail(e, "batch: learned sort");
-      // When the learned sort keeps the result, `sorted` must not be the
-      // passes' input: with an even pass count it is ka itself, so the
-      // learned path is only offered for odd pass counts (host check).
+      // The learned result must not land in the passes' input (ka): with an
+      // even pass count `sorted` is ka, so the learned path is offered for
+      // odd pass counts only (host check).
     }
     uint32_t* a = ka;
     uint32_t* b = kb;
@@ -717,7 +717,7 @@ int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* p
     e = cudaMemsetAsync(d_cloud_counts, 0, 16 * (size_t)P->C, s);
   }
   if (e == cudaSuccess && lb && lb->d_stats)
-    e = cudaMemcpyAsync(lb->d_stats, lb->ws, 2 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+    e = cudaMemcpyAsync(lb->d_stats, lb->ws, sizeof(LsortStats), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e == cudaSuccess ? OCT_OK : batch_fail(e, "oct_build_octree_batch");
 }
@@ -738,7 +738,7 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
 OCT_API size_t oct_batch_learned_workspace_bytes(const oct_batch_plan* P, int n_buckets) {
   if (!P || n_buckets < 1 || n_buckets > 65536) return 0;
   return octgb::align_up(P->ws_bytes, 256) + lbatch_flag_bytes() +
-         octgb::lbatch_scratch_bytes((int)P->sort_tiles.size(), P->C, n_buckets);
+         octgb::lbatch_scratch_bytes((int)P->sort_tiles.size(), P->C, n_buckets, P->N);
 }
 
 OCT_API int oct_build_octree_batch_learned(const oct_batch_plan* P, const void* d_tables,

@@ -596,17 +596,33 @@ __global__ void __launch_bounds__(256)
 // ----------------------------------------------------- batched learned sort --
 // The clouds of a batch share one model over their own (per-cloud
 // quantised) Morton codes. Bucket b of cloud c holds the cloud's keys with
-// bucket(key) == b, so each cloud's keys sorted bucket by bucket are the
-// cloud's sorted keys; duplicates are kept (the batched unique that follows
-// removes them).
-//   lb_hist     per sort tile (tiles never cross clouds): bucket counts
-//   lb_scan     per cloud: every tile's offset in every bucket, bucket starts
-//               and sizes; a bucket above kBkCache keys sets `fallback`
-//   lb_scatter  per tile: each key to its bucket (any order inside it)
-//   lb_bucket   one CTA per (cloud, bucket): the stable shared-memory radix
-//               sort of the bucket's keys (bucket_radix_sort), in place
-// With `fallback` set, lb_scatter and lb_bucket return at once and the plain
-// LSD passes (gated on the same flag) sort the batch instead.
+// bucket(key) == b, so the unique keys of each cloud's buckets, in bucket
+// order, are the cloud's sorted unique keys:
+//   lb_hist      per sort tile (tiles never cross clouds): bucket counts of
+//                the keys left after dropping repeats within each warp's 32
+//   lb_scan      per cloud: every tile's offset in every bucket, bucket starts
+//   lb_scatter   per tile: each of those keys to its bucket (any order)
+//   lsort_bucket one CTA per (cloud, bucket), the single-cloud bucket kernel:
+//                the bucket's sorted unique keys at its front (bitmap, radix
+//                or bitonic form); a bucket that fits no form sets fallback
+//   lb_uscan     per cloud: offsets of the buckets' unique runs
+//   lb_compact   the runs, packed per cloud at the cloud's start
+//   lb_pad       the rest of each cloud's range filled with its largest key,
+//                so the cloud's range holds sorted keys (its unique keys,
+//                then copies of the last one) for the batched unique stage
+// With fallback set, the last three return at once and the plain LSD passes
+// (gated on the same flag) sort the original keys instead.
+// Only the unique keys of each cloud are needed, so of the equal keys among
+// a warp's 32 consecutive keys (in scan order) only the lowest lane's goes to
+// a bucket: dense clusters (many points in one cell) shrink before the
+// buckets see them. The histogram and the scatter group the keys the same
+// way, so their counts agree. Lanes past the tile hold 2^32 - 1, which no
+// code reaches.
+__device__ __forceinline__ bool lb_first_of_its_key(uint32_t k) {
+  const uint32_t peers = __match_any_sync(0xffffffffu, k);
+  return k != 0xffffffffu && (peers & lanemask_lt()) == 0;
+}
+
 __global__ void __launch_bounds__(256)
     lb_hist_kernel(const uint32_t* __restrict__ keys, const int4* __restrict__ tiles,
                    const char* __restrict__ blob, LcdfLayout L, int nb,
@@ -617,8 +633,12 @@ __global__ void __launch_bounds__(256)
   const BucketLookup q = load_lookup(blob, L, nb, s_hist + nb,
                                      reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
   const int4 d = tiles[blockIdx.x];
-  for (int i = d.x + (int)threadIdx.x; i < d.y; i += blockDim.x)
-    atomicAdd(&s_hist[bucket_of(q, keys[i])], 1u);
+  const int lane = threadIdx.x & 31;
+  for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
+    const int i = base + lane;
+    const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;  // no code reaches 2^32 - 1
+    if (lb_first_of_its_key(k)) atomicAdd(&s_hist[bucket_of(q, k)], 1u);
+  }
   __syncthreads();
   uint32_t* row = tile_off + (size_t)blockIdx.x * nb;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) row[b] = s_hist[b];
@@ -626,9 +646,8 @@ __global__ void __launch_bounds__(256)
 
 __global__ void __launch_bounds__(1024)
     lb_scan_kernel(const int* __restrict__ start, const int* __restrict__ cloud_tile0, int nb,
-                   uint32_t* __restrict__ tile_off, uint32_t* __restrict__ bstart,
-                   uint32_t* __restrict__ bcount, uint32_t* __restrict__ fallback,
-                   uint32_t* __restrict__ max_bucket) {
+                   int C, uint32_t* __restrict__ tile_off, uint32_t* __restrict__ bstart,
+                   LsortStats* __restrict__ stats) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   extern __shared__ __align__(16) unsigned char sm[];
@@ -655,27 +674,23 @@ __global__ void __launch_bounds__(1024)
   for (int b = b0; b < min(b0 + per, nb); ++b) sum += tot[b];
   uint32_t run = block_exclusive_sum<1024>(sum, s_warp, &s_total) + (uint32_t)start[c];
   for (int b = b0; b < min(b0 + per, nb); ++b) {
+    const uint32_t t = tot[b];
     bstart[(size_t)c * nb + b] = run;
-    bcount[(size_t)c * nb + b] = tot[b];
     tot[b] = run;
-    run += bcount[(size_t)c * nb + b];
+    run += t;
   }
+  if (c == C - 1 && threadIdx.x == 0) bstart[(size_t)C * nb] = (uint32_t)start[C];
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     for (int t = t0; t < t1; ++t) tile_off[(size_t)t * nb + b] += tot[b];
   big = __reduce_max_sync(0xffffffffu, big);
-  if ((threadIdx.x & 31) == 0 && big) {
-    atomicMax(max_bucket, big);
-    if (big > (uint32_t)kBkCache) atomicOr(fallback, 1u);
-  }
+  if ((threadIdx.x & 31) == 0 && big) atomicMax(&stats->max_bucket, big);
 }
 
 __global__ void __launch_bounds__(256)
     lb_scatter_kernel(const uint32_t* __restrict__ keys, uint32_t* __restrict__ out,
                       const int4* __restrict__ tiles, const char* __restrict__ blob, LcdfLayout L,
-                      int nb, const uint32_t* __restrict__ tile_off,
-                      const uint32_t* __restrict__ fallback) {
-  if (*fallback) return;
+                      int nb, const uint32_t* __restrict__ tile_off) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
   const uint32_t* row = tile_off + (size_t)blockIdx.x * nb;
@@ -683,78 +698,98 @@ __global__ void __launch_bounds__(256)
   const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
                                      reinterpret_cast<uint16_t*>(cursor + 2 * nb));
   const int4 d = tiles[blockIdx.x];
-  for (int i = d.x + (int)threadIdx.x; i < d.y; i += blockDim.x) {
-    const uint32_t k = keys[i];
-    out[atomicAdd(&cursor[bucket_of(q, k)], 1u)] = k;
+  const int lane = threadIdx.x & 31;
+  for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
+    const int i = base + lane;
+    const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;
+    if (lb_first_of_its_key(k)) out[atomicAdd(&cursor[bucket_of(q, k)], 1u)] = k;
   }
 }
 
-__global__ void __launch_bounds__(kBkThreads, 3)
-    lb_bucket_kernel(uint32_t* __restrict__ keys, const uint32_t* __restrict__ bstart,
-                     const uint32_t* __restrict__ bcount, const uint32_t* __restrict__ fallback) {
-  if (*fallback) return;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  BucketSmem& S = *reinterpret_cast<BucketSmem*>(sm_raw);
-  const int cnt = (int)bcount[blockIdx.x];
-  if (cnt <= 1) return;
-  uint32_t* g = keys + bstart[blockIdx.x];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  uint32_t kmin = 0xffffffffu, kmax = 0;
-  for (int i = tid; i < cnt; i += kBkThreads) {
-    const uint32_t k = g[i];
-    S.buf[i] = k;
-    kmin = min(kmin, k);
-    kmax = max(kmax, k);
+// Per cloud: unique-run offsets (absolute positions) and the cloud's U.
+__global__ void __launch_bounds__(1024)
+    lb_uscan_kernel(const int* __restrict__ start, int nb, const uint32_t* __restrict__ ucount,
+                    uint32_t* __restrict__ uoff, uint32_t* __restrict__ ucloud,
+                    const LsortStats* __restrict__ stats) {
+  if (stats->fallback) return;
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const int c = blockIdx.x;
+  const int per = (nb + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  const uint32_t* uc = ucount + (size_t)c * nb;
+  uint32_t sum = 0;
+  for (int b = b0; b < min(b0 + per, nb); ++b) sum += uc[b];
+  uint32_t run = block_exclusive_sum<1024>(sum, s_warp, &s_total) + (uint32_t)start[c];
+  for (int b = b0; b < min(b0 + per, nb); ++b) {
+    uoff[(size_t)c * nb + b] = run;
+    run += uc[b];
   }
-  kmin = __reduce_min_sync(0xffffffffu, kmin);
-  kmax = __reduce_max_sync(0xffffffffu, kmax);
-  if (lane == 0) {
-    S.red[0][wid] = kmin;
-    S.red[1][wid] = kmax;
-  }
-  __syncthreads();
-  if (wid == 0) {
-    uint32_t a = lane < kBkWarps ? S.red[0][lane] : 0xffffffffu;
-    uint32_t z = lane < kBkWarps ? S.red[1][lane] : 0u;
-    a = __reduce_min_sync(0xffffffffu, a);
-    z = __reduce_max_sync(0xffffffffu, z);
-    if (lane == 0) {
-      S.misc[1] = a;
-      S.misc[2] = z;
-    }
-  }
-  __syncthreads();
-  kmin = S.misc[1];
-  kmax = S.misc[2];
-  if (kmin == kmax) return;  // all keys equal: already sorted
-  const int bits = 32 - __clz(kmax - kmin);
-  const uint32_t* sorted = bucket_radix_sort(S.buf, S.buf + kBkCache, cnt, kmin, bits, S);
-  for (int i = tid; i < cnt; i += kBkThreads) g[i] = sorted[i];
+  if (threadIdx.x == 0) ucloud[c] = s_total;
 }
 
-size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb) {
-  return align_up(4 * (size_t)n_tiles * nb, 256) + 2 * align_up(4 * (size_t)n_clouds * nb, 256);
+__global__ void __launch_bounds__(256)
+    lb_compact_kernel(const uint32_t* __restrict__ bkeys, const uint32_t* __restrict__ bstart,
+                      const uint32_t* __restrict__ ucount, const uint32_t* __restrict__ uoff,
+                      uint32_t* __restrict__ out, const LsortStats* __restrict__ stats) {
+  if (stats->fallback) return;
+  const int g = blockIdx.x;
+  const uint32_t n = ucount[g];
+  const uint32_t* src = bkeys + bstart[g];
+  uint32_t* dst = out + uoff[g];
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(256)
+    lb_pad_kernel(const int* __restrict__ start, const uint32_t* __restrict__ ucloud,
+                  uint32_t* __restrict__ out, const LsortStats* __restrict__ stats) {
+  if (stats->fallback) return;
+  const int c = blockIdx.x;
+  const int s0 = start[c], s1 = start[c + 1];
+  const int u = (int)ucloud[c];
+  if (u == 0) return;
+  const uint32_t last = out[s0 + u - 1];
+  for (int i = s0 + u + (int)threadIdx.x; i < s1; i += blockDim.x) out[i] = last;
+}
+
+size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb, int n) {
+  const size_t g = (size_t)n_clouds * nb;
+  return align_up(4 * (size_t)n_tiles * nb, 256) + align_up(4 * (g + 1), 256) +
+         2 * align_up(4 * g, 256) + align_up(4 * (size_t)n_clouds, 256) +
+         align_up(4 * (size_t)(n > 0 ? n : 1), 256);
 }
 
 cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s) {
   if (a.n_tiles <= 0) return cudaSuccess;
+  const size_t G = (size_t)a.C * a.nb;
   char* w = static_cast<char*>(a.scratch);
-  uint32_t* tile_off = reinterpret_cast<uint32_t*>(w);
-  uint32_t* bstart = reinterpret_cast<uint32_t*>(w + align_up(4 * (size_t)a.n_tiles * a.nb, 256));
-  uint32_t* bcount = bstart + align_up(4 * (size_t)a.C * a.nb, 256) / 4;
+  auto take = [&](size_t bytes) {
+    char* p = w;
+    w += align_up(bytes, 256);
+    return reinterpret_cast<uint32_t*>(p);
+  };
+  uint32_t* tile_off = take(4 * (size_t)a.n_tiles * a.nb);
+  uint32_t* bstart = take(4 * (G + 1));
+  uint32_t* ucount = take(4 * G);
+  uint32_t* uoff = take(4 * G);
+  uint32_t* ucloud = take(4 * (size_t)a.C);
+  uint32_t* bkeys = take(4 * (size_t)(a.n > 0 ? a.n : 1));
   const size_t hsm = lsort_hist_smem(a.nb, a.L.max_knots);
   if (hsm > (size_t)kLsortMaxSmem) return cudaErrorInvalidValue;
   cudaError_t e = set_smem_limit(lb_hist_kernel, (int)hsm);
   if (e == cudaSuccess) e = set_smem_limit(lb_scatter_kernel, (int)hsm);
-  if (e == cudaSuccess) e = set_smem_limit(lb_bucket_kernel, (int)sizeof(BucketSmem));
+  if (e == cudaSuccess) e = set_smem_limit(lsort_bucket_kernel, (int)sizeof(BucketSmem));
   if (e != cudaSuccess) return e;
   lb_hist_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, a.tiles, a.blob, a.L, a.nb, tile_off);
-  lb_scan_kernel<<<a.C, 1024, 4 * (size_t)a.nb, s>>>(a.start, a.cloud_tile0, a.nb, tile_off,
-                                                     bstart, bcount, a.fallback, a.max_bucket);
-  lb_scatter_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, a.out, a.tiles, a.blob, a.L, a.nb,
-                                                tile_off, a.fallback);
-  lb_bucket_kernel<<<a.C * a.nb, kBkThreads, sizeof(BucketSmem), s>>>(a.out, bstart, bcount,
-                                                                      a.fallback);
+  lb_scan_kernel<<<a.C, 1024, 4 * (size_t)a.nb, s>>>(a.start, a.cloud_tile0, a.nb, a.C, tile_off,
+                                                     bstart, a.stats);
+  lb_scatter_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, bkeys, a.tiles, a.blob, a.L, a.nb,
+                                                tile_off);
+  lsort_bucket_kernel<<<(unsigned)G, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, bstart, ucount,
+                                                                          a.stats);
+  lb_uscan_kernel<<<a.C, 1024, 0, s>>>(a.start, a.nb, ucount, uoff, ucloud, a.stats);
+  lb_compact_kernel<<<(unsigned)G, 256, 0, s>>>(bkeys, bstart, ucount, uoff, a.out, a.stats);
+  lb_pad_kernel<<<a.C, 256, 0, s>>>(a.start, ucloud, a.out, a.stats);
   return cudaGetLastError();
 }
 

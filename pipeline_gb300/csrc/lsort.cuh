@@ -41,10 +41,11 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
                          uint32_t* out, int* d_unique, uint32_t* status, cudaStream_t s,
                          Recorder* rec);
 
-// Learned bucket sort of a batch of clouds (keys keep their duplicates):
-// each cloud's keys sorted, in `out`, unless a bucket exceeds the shared-memory
-// sort's capacity, which sets *fallback (zeroed by the caller) and leaves
-// `out` to a sort gated on that flag.
+// Learned bucket sort of a batch of clouds: each cloud's range of `out`
+// receives its sorted unique keys followed by copies of its largest key
+// (sorted keys, for the batched unique stage), unless a bucket fits none of
+// the bucket forms, which sets stats->fallback and leaves `out` to a sort
+// gated on that flag. `keys` is not modified.
 struct LbatchArgs {
   const uint32_t* keys;      // cloud-concatenated Morton codes
   uint32_t* out;             // cloud-concatenated sorted codes
@@ -53,14 +54,14 @@ struct LbatchArgs {
   const int* start;          // [C + 1] cloud starts
   const int* cloud_tile0;    // [C + 1] first tile of each cloud
   int C;
+  int n;                     // keys in the batch
   const char* blob;          // the model
   LcdfLayout L;
   int nb;                    // buckets per cloud
-  void* scratch;             // lbatch_scratch_bytes(n_tiles, C, nb), not zeroed
-  uint32_t* fallback;        // zeroed before the call
-  uint32_t* max_bucket;      // zeroed before the call
+  void* scratch;             // lbatch_scratch_bytes(n_tiles, C, nb, n), not zeroed
+  LsortStats* stats;         // zeroed before the call (fallback, max_bucket, bucket forms)
 };
-size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb);
+size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb, int n);
 cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s);
 
 }  // namespace octgb

@@ -68,7 +68,7 @@ def test_frames_learned_batched_matches_oracle_and_plain(frames):
     b, pts, mn, rg = _build(test, mins[8:], ranges[8:], model, 64)
     b.build(pts, mn, rg)
     st = b.learned_stats()
-    assert st["fallback"] == 0 and 0 < st["max_bucket"] <= 8192, st
+    assert st["fallback"] == 0 and st["max_bucket"] > 0, st
     _check_all(b, test, mins[8:], ranges[8:])
     plain, pts2, mn2, rg2 = _build(test, mins[8:], ranges[8:])
     plain.build(pts2, mn2, rg2)
@@ -78,14 +78,16 @@ def test_frames_learned_batched_matches_oracle_and_plain(frames):
     assert torch.equal(plain.codes, b.codes)
 
 
-def test_learned_batched_falls_back_when_a_bucket_overflows(frames):
+def test_learned_batched_falls_back_when_a_bucket_fits_no_form(frames):
+    """One bucket per frame: far more unique keys than the bitonic form holds,
+    over a span wider than the bitmap form covers, so the LSD passes run."""
     fr, mins, ranges = frames
     model = _fit(fr[:4], mins[:4], ranges[:4], nb=1, segments=64)
     test = fr[30:36]
     b, pts, mn, rg = _build(test, mins[30:36], ranges[30:36], model, 1)
     b.build(pts, mn, rg)
     st = b.learned_stats()
-    assert st["fallback"] == 1 and st["max_bucket"] > 8192, st
+    assert st["fallback"] == 1 and st["max_bucket"] > 16384, st
     _check_all(b, test, mins[30:36], ranges[30:36])
 
 
