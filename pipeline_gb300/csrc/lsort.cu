@@ -398,7 +398,8 @@ __device__ __forceinline__ uint32_t heads_emit(const uint32_t* a, int seg0, int 
 // another. A scan of the counts and a copy kernel then pack the runs.
 __global__ void __launch_bounds__(kBkThreads, 3)
     lsort_bucket_kernel(uint32_t* __restrict__ bkeys, const uint32_t* __restrict__ starts,
-                        uint32_t* __restrict__ ucount, LsortStats* __restrict__ stats) {
+                        uint32_t* __restrict__ ucount, LsortStats* __restrict__ stats,
+                        const uint32_t* __restrict__ counts = nullptr) {
   // `skip` is final before this kernel starts; `fallback` may still be set by
   // a failing bucket.
   if (stats->skip) return;
@@ -406,8 +407,9 @@ __global__ void __launch_bounds__(kBkThreads, 3)
   BucketSmem& S = *reinterpret_cast<BucketSmem*>(sm_raw);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int b = blockIdx.x;
-  const uint32_t lo = starts[b], hi = starts[b + 1];
-  const int cnt = (int)(hi - lo);
+  // bucket b: keys [starts[b], starts[b] + counts[b]), or up to starts[b + 1]
+  const uint32_t lo = starts[b];
+  const int cnt = (int)(counts ? counts[b] : starts[b + 1] - lo);
   const bool cached = cnt <= kBkCache;
   // keys -> cache, and the key span of the bucket
   uint32_t kmin = 0xffffffffu, kmax = 0;
@@ -647,7 +649,7 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(1024)
     lb_scan_kernel(const int* __restrict__ start, const int* __restrict__ cloud_tile0, int nb,
                    int C, uint32_t* __restrict__ tile_off, uint32_t* __restrict__ bstart,
-                   LsortStats* __restrict__ stats) {
+                   uint32_t* __restrict__ bcount, LsortStats* __restrict__ stats) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   extern __shared__ __align__(16) unsigned char sm[];
@@ -676,10 +678,10 @@ __global__ void __launch_bounds__(1024)
   for (int b = b0; b < min(b0 + per, nb); ++b) {
     const uint32_t t = tot[b];
     bstart[(size_t)c * nb + b] = run;
+    bcount[(size_t)c * nb + b] = t;
     tot[b] = run;
     run += t;
   }
-  if (c == C - 1 && threadIdx.x == 0) bstart[(size_t)C * nb] = (uint32_t)start[C];
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     for (int t = t0; t < t1; ++t) tile_off[(size_t)t * nb + b] += tot[b];
@@ -754,8 +756,8 @@ __global__ void __launch_bounds__(256)
 
 size_t lbatch_scratch_bytes(int n_tiles, int n_clouds, int nb, int n) {
   const size_t g = (size_t)n_clouds * nb;
-  return align_up(4 * (size_t)n_tiles * nb, 256) + align_up(4 * (g + 1), 256) +
-         2 * align_up(4 * g, 256) + align_up(4 * (size_t)n_clouds, 256) +
+  return align_up(4 * (size_t)n_tiles * nb, 256) + 4 * align_up(4 * g, 256) +
+         align_up(4 * (size_t)n_clouds, 256) +
          align_up(4 * (size_t)(n > 0 ? n : 1), 256);
 }
 
@@ -769,7 +771,8 @@ cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s) {
     return reinterpret_cast<uint32_t*>(p);
   };
   uint32_t* tile_off = take(4 * (size_t)a.n_tiles * a.nb);
-  uint32_t* bstart = take(4 * (G + 1));
+  uint32_t* bstart = take(4 * G);
+  uint32_t* bcount = take(4 * G);
   uint32_t* ucount = take(4 * G);
   uint32_t* uoff = take(4 * G);
   uint32_t* ucloud = take(4 * (size_t)a.C);
@@ -782,11 +785,11 @@ cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   lb_hist_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, a.tiles, a.blob, a.L, a.nb, tile_off);
   lb_scan_kernel<<<a.C, 1024, 4 * (size_t)a.nb, s>>>(a.start, a.cloud_tile0, a.nb, a.C, tile_off,
-                                                     bstart, a.stats);
+                                                     bstart, bcount, a.stats);
   lb_scatter_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, bkeys, a.tiles, a.blob, a.L, a.nb,
                                                 tile_off);
   lsort_bucket_kernel<<<(unsigned)G, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, bstart, ucount,
-                                                                          a.stats);
+                                                                          a.stats, bcount);
   lb_uscan_kernel<<<a.C, 1024, 0, s>>>(a.start, a.nb, ucount, uoff, ucloud, a.stats);
   lb_compact_kernel<<<(unsigned)G, 256, 0, s>>>(bkeys, bstart, ucount, uoff, a.out, a.stats);
   lb_pad_kernel<<<a.C, 256, 0, s>>>(a.start, ucloud, a.out, a.stats);
