@@ -113,6 +113,22 @@ class BatchOctreeBuilder:
             self.workspace.numel(), C.c_void_p(s.cuda_stream))
         _lib.check(rc, "oct_build_octree_batch")
 
+    def same_results(self, other: "BatchOctreeBuilder") -> bool:
+        """True when both builders' last builds gave the same counts and, per
+        cloud, the same codes [0, U) and OctNodes [0, M) (the rest of each
+        cloud's output range is not defined)."""
+        if not torch.equal(self.counts, other.counts):
+            return False
+        counts = self.cloud_counts()
+        for c in range(self.n_clouds):
+            u, m = int(counts[c][0]), int(counts[c][2])
+            cs, ns = int(self.start[c]), int(self.node_start[c])
+            if not torch.equal(self.codes[cs:cs + u], other.codes[cs:cs + u]):
+                return False
+            if not torch.equal(self.nodes[ns:ns + m], other.nodes[ns:ns + m]):
+                return False
+        return True
+
     def learned_stats(self) -> dict:
         """Learned stage of the last build: fallback (1 if the LSD passes
         sorted the batch), the largest bucket, buckets per bucket form."""

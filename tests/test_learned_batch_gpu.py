@@ -73,9 +73,7 @@ def test_frames_learned_batched_matches_oracle_and_plain(frames):
     plain, pts2, mn2, rg2 = _build(test, mins[8:], ranges[8:])
     plain.build(pts2, mn2, rg2)
     torch.cuda.synchronize()
-    assert torch.equal(plain.counts, b.counts)
-    assert torch.equal(plain.nodes, b.nodes)
-    assert torch.equal(plain.codes, b.codes)
+    assert plain.same_results(b)
 
 
 def test_learned_batched_falls_back_when_a_bucket_fits_no_form(frames):
