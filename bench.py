@@ -740,9 +740,9 @@ def frames_workload(dev, flush, reps):
         overflow.append(st["overflow_frac"])
         exact &= r["oct_nodes"].tobytes() == b.cloud_result(c, counts)["oct_nodes"].tobytes()
         exact &= r["oct_nodes"].tobytes() == lr_["oct_nodes"].tobytes()
-    # learned + batched: one model (64 buckets per frame) fit on frames 0-31
+    # learned + batched: one model (32 buckets per frame) fit on frames 0-31
     # drives the batched build's sort for frames 32-255
-    nb_lb = 64
+    nb_lb = 32
     t0 = time.perf_counter()
     model_lb = LearnedCDF(max_segments=1024).fit(sample, n_segments=1024, steps=100, lr=0.05,
                                                  n_buckets=nb_lb)

@@ -30,6 +30,8 @@
 // key array, identical to the plain path's.
 #include <stdio.h>
 
+#include <algorithm>
+
 #include "learned.cuh"
 #include "lsort.cuh"
 
@@ -625,25 +627,31 @@ __device__ __forceinline__ bool lb_first_of_its_key(uint32_t k) {
   return k != 0xffffffffu && (peers & lanemask_lt()) == 0;
 }
 
+// CTAs walk the tiles from a capped grid, so each stages the model's lookup
+// tables once for several tiles.
 __global__ void __launch_bounds__(256)
-    lb_hist_kernel(const uint32_t* __restrict__ keys, const int4* __restrict__ tiles,
+    lb_hist_kernel(const uint32_t* __restrict__ keys, const int4* __restrict__ tiles, int n_tiles,
                    const char* __restrict__ blob, LcdfLayout L, int nb,
                    uint32_t* __restrict__ tile_off) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* s_hist = reinterpret_cast<uint32_t*>(sm);
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0;
   const BucketLookup q = load_lookup(blob, L, nb, s_hist + nb,
                                      reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
-  const int4 d = tiles[blockIdx.x];
   const int lane = threadIdx.x & 31;
-  for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
-    const int i = base + lane;
-    const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;  // no code reaches 2^32 - 1
-    if (lb_first_of_its_key(k)) atomicAdd(&s_hist[bucket_of(q, k)], 1u);
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0;
+    __syncthreads();
+    const int4 d = tiles[t];
+    for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
+      const int i = base + lane;
+      const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;  // no code reaches 2^32 - 1
+      if (lb_first_of_its_key(k)) atomicAdd(&s_hist[bucket_of(q, k)], 1u);
+    }
+    __syncthreads();
+    uint32_t* row = tile_off + (size_t)t * nb;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) row[b] = s_hist[b];
+    __syncthreads();
   }
-  __syncthreads();
-  uint32_t* row = tile_off + (size_t)blockIdx.x * nb;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) row[b] = s_hist[b];
 }
 
 __global__ void __launch_bounds__(1024)
@@ -691,20 +699,24 @@ __global__ void __launch_bounds__(1024)
 
 __global__ void __launch_bounds__(256)
     lb_scatter_kernel(const uint32_t* __restrict__ keys, uint32_t* __restrict__ out,
-                      const int4* __restrict__ tiles, const char* __restrict__ blob, LcdfLayout L,
-                      int nb, const uint32_t* __restrict__ tile_off) {
+                      const int4* __restrict__ tiles, int n_tiles, const char* __restrict__ blob,
+                      LcdfLayout L, int nb, const uint32_t* __restrict__ tile_off) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
-  const uint32_t* row = tile_off + (size_t)blockIdx.x * nb;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) cursor[b] = row[b];
   const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
                                      reinterpret_cast<uint16_t*>(cursor + 2 * nb));
-  const int4 d = tiles[blockIdx.x];
   const int lane = threadIdx.x & 31;
-  for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
-    const int i = base + lane;
-    const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;
-    if (lb_first_of_its_key(k)) out[atomicAdd(&cursor[bucket_of(q, k)], 1u)] = k;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const uint32_t* row = tile_off + (size_t)t * nb;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) cursor[b] = row[b];
+    __syncthreads();
+    const int4 d = tiles[t];
+    for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
+      const int i = base + lane;
+      const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;
+      if (lb_first_of_its_key(k)) out[atomicAdd(&cursor[bucket_of(q, k)], 1u)] = k;
+    }
+    __syncthreads();
   }
 }
 
@@ -783,11 +795,12 @@ cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s) {
   if (e == cudaSuccess) e = set_smem_limit(lb_scatter_kernel, (int)hsm);
   if (e == cudaSuccess) e = set_smem_limit(lsort_bucket_kernel, (int)sizeof(BucketSmem));
   if (e != cudaSuccess) return e;
-  lb_hist_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, a.tiles, a.blob, a.L, a.nb, tile_off);
+  const int tgrid = std::min(a.n_tiles, device_sm_count() * 6);
+  lb_hist_kernel<<<tgrid, 256, hsm, s>>>(a.keys, a.tiles, a.n_tiles, a.blob, a.L, a.nb, tile_off);
   lb_scan_kernel<<<a.C, 1024, 4 * (size_t)a.nb, s>>>(a.start, a.cloud_tile0, a.nb, a.C, tile_off,
                                                      bstart, bcount, a.stats);
-  lb_scatter_kernel<<<a.n_tiles, 256, hsm, s>>>(a.keys, bkeys, a.tiles, a.blob, a.L, a.nb,
-                                                tile_off);
+  lb_scatter_kernel<<<tgrid, 256, hsm, s>>>(a.keys, bkeys, a.tiles, a.n_tiles, a.blob, a.L, a.nb,
+                                            tile_off);
   lsort_bucket_kernel<<<(unsigned)G, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, bstart, ucount,
                                                                           a.stats, bcount);
   lb_uscan_kernel<<<a.C, 1024, 0, s>>>(a.start, a.nb, ucount, uoff, ucloud, a.stats);
