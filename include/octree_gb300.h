@@ -395,6 +395,12 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* plan, const void* d_tab
                                    int32_t* d_cloud_counts, void* workspace,
                                    size_t workspace_bytes, oct_stream_t stream);
 
+/* Scheduling of the batched build's octree-stage kernels (prefix sum, emit,
+ * finalize): 1 (default) persistent CTAs take their tiles from an atomic work
+ * queue; 0 one CTA per tile by block index. Results are the same; for
+ * measurement. Applies to later builds in this process. */
+OCT_API int oct_set_batch_work_queue(int on);
+
 /* Learned + batched build (no counterpart in the reference): the batched
  * build with stage 2 done by one learned CDF model shared by the clouds
  * (fit on their own per-cloud Morton codes, oct_lcdf_fit): per cloud, each

@@ -124,6 +124,7 @@ SIGNATURES = {
     "oct_batch_upload_tables": (I, [P, P, P]),
     "oct_build_octree_batch": (I, [P, P, P, P, P, C.POINTER(OctBuildOutputs), P, P, Z, P]),
     "oct_batch_learned_workspace_bytes": (Z, [P, I]),
+    "oct_set_batch_work_queue": (I, [I]),
     "oct_build_octree_batch_learned": (I, [P, P, P, P, P, P, I, I, C.POINTER(OctBuildOutputs), P,
                                            P, P, Z, P]),
     "oct_build_sort_form": (I, [P, I, I, P]),

@@ -192,6 +192,18 @@ __global__ void __launch_bounds__(32 * kTsGroups)
   }
 }
 
+// --------------------------------------------------------- tile schedule --
+// A batched kernel's tiles: one per CTA by block index (queue == nullptr), or
+// taken from an atomic work queue (zeroed before the build) by persistent
+// CTAs, one at a time, until they run out. The CTA calls this between tiles.
+__device__ __forceinline__ int next_tile(uint32_t* queue, int& round, int* s_tile) {
+  if (!queue) return round++ == 0 ? (int)blockIdx.x : 0x7fffffff;
+  __syncthreads();  // the previous tile is done with *s_tile
+  if (threadIdx.x == 0) *s_tile = (int)atomicAdd(queue, 1u);
+  __syncthreads();
+  return *s_tile;
+}
+
 // ------------------------------------------------------------ prefix sum --
 // Inclusive prefix sum of each cloud's edge counts (written by the tree
 // kernels with their per-tile sums, scanned into tile_prefix), and each
@@ -200,7 +212,10 @@ __global__ void __launch_bounds__(256)
     batch_prefix_sum_kernel(BatchDev B, const int* __restrict__ unique_c,
                             const int* __restrict__ ec, int* __restrict__ ps_out,
                             int* __restrict__ max_slot_c, const uint32_t* __restrict__ tile_prefix,
-                            OctTags tags) {
+                            OctTags tags, uint32_t* __restrict__ queue) {
+  __shared__ int s_tile;
+  int round = 0;
+  for (int t = next_tile(queue, round, &s_tile); t < B.T4; t = next_tile(queue, round, &s_tile)) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ int s_max[8];
@@ -211,12 +226,11 @@ __global__ void __launch_bounds__(256)
   // entry j at j + j / 32, conflict-free both ways)
   __shared__ int s_v[256 * ITEMS + 256 * ITEMS / 32];
   const int tid = threadIdx.x;
-  const int t = blockIdx.x;
   const int4 d = B.tiles4k[t];
   const int c = d.z, cs = B.start[c];
   const int n = max(unique_c[c] - 1, 0);  // radix nodes of this cloud
   const int lo = d.x - cs;                // first node of the tile (cloud-local)
-  if (lo >= n) return;
+  if (lo >= n) continue;
   const int valid = min(256 * ITEMS, n - lo);
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
@@ -279,6 +293,7 @@ __global__ void __launch_bounds__(256)
     c4[2 * g + 1] = make_uint4(0, 0, 0, 0);
     tags.owner[g] = 0;
     tags.mask[g] = 0;
+  }
   }
 }
 
@@ -346,61 +361,71 @@ __device__ __forceinline__ OctTags cloud_tags(const BatchOctDev& O, const CloudS
 
 // One CTA per 4,096-node tile of a cloud.
 __global__ void __launch_bounds__(256, 6)
-    batch_oct_emit_kernel(BatchDev B, BatchOctDev O, uint32_t* __restrict__ status) {
-  const int4 d = B.tiles4k[blockIdx.x];
-  const int c = d.z;
-  const CloudSizes z = cloud_sizes(B, O, c);
-  if (!z.fits) {
-    if ((int)blockIdx.x == d.w && threadIdx.x == 0) raise_status(status, kStatusCapacity);
-    return;
+    batch_oct_emit_kernel(BatchDev B, BatchOctDev O, uint32_t* __restrict__ status,
+                          uint32_t* __restrict__ queue) {
+  __shared__ int s_tile;
+  int round = 0;
+  for (int k = next_tile(queue, round, &s_tile); k < B.T4; k = next_tile(queue, round, &s_tile)) {
+    const int4 d = B.tiles4k[k];
+    const int c = d.z;
+    const CloudSizes z = cloud_sizes(B, O, c);
+    if (!z.fits) {
+      if (k == d.w && threadIdx.x == 0) raise_status(status, kStatusCapacity);
+      continue;
+    }
+    const int cs = B.start[c];
+    const int end = min(d.y - cs, z.n_brt);
+    const OctArgs a = cloud_view(B, O, z);
+    const OctTags t = cloud_tags(O, z);
+    Sizes zz;
+    zz.n_brt = z.n_brt;
+    zz.n_oct = z.n_oct;
+    zz.fits = true;
+    for (int i = d.x - cs + (int)threadIdx.x; i < end; i += 256)
+      emit_node(kOctMake | kOctLink, i, a, t, zz, status);
   }
-  const int cs = B.start[c];
-  const int end = min(d.y - cs, z.n_brt);
-  const OctArgs a = cloud_view(B, O, z);
-  const OctTags t = cloud_tags(O, z);
-  Sizes zz;
-  zz.n_brt = z.n_brt;
-  zz.n_oct = z.n_oct;
-  zz.fits = true;
-  for (int i = d.x - cs + (int)threadIdx.x; i < end; i += 256)
-    emit_node(kOctMake | kOctLink, i, a, t, zz, status);
 }
 
 // One CTA per 256 OctNode slots of a cloud.
 __global__ void __launch_bounds__(kFinThreads, 6)
-    batch_oct_finalize_kernel(BatchDev B, BatchOctDev O) {
+    batch_oct_finalize_kernel(BatchDev B, BatchOctDev O, uint32_t* __restrict__ queue) {
   __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
-  const int4 d = B.slot_tiles[blockIdx.x];
-  const CloudSizes z = cloud_sizes(B, O, d.z);
-  const int p0 = d.x - z.ns;
-  const int count = min(d.y - d.x, z.n_oct - p0);
-  if (!z.fits || z.n_brt < 1 || count <= 0) return;
-  const OctArgs a = cloud_view(B, O, z);
-  const int p = p0 + (int)threadIdx.x;
-  if ((int)threadIdx.x < count)
-    finalize_slot(true, p, a, cloud_tags(O, z), a.prefix_n[0] / 3,
-                  s_nodes + threadIdx.x * kNodeWords);
-  bulk_fence_writes();
-  __syncthreads();
-  int* dst = reinterpret_cast<int*>(O.nodes + d.x);
-  const int words = count * kNodeWords;
-  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0 && (words & 3) == 0) {
-    // one bulk copy of the staged block (the TMA engine writes it)
-    if (threadIdx.x == 0) {
-      bulk_store_s2g(dst, s_nodes, (uint32_t)words * 4u);
-      bulk_wait_all();
+  __shared__ int s_tile;
+  int round = 0;
+  for (int k = next_tile(queue, round, &s_tile); k < B.Tn; k = next_tile(queue, round, &s_tile)) {
+    const int4 d = B.slot_tiles[k];
+    const CloudSizes z = cloud_sizes(B, O, d.z);
+    const int p0 = d.x - z.ns;
+    const int count = min(d.y - d.x, z.n_oct - p0);
+    if (!z.fits || z.n_brt < 1 || count <= 0) continue;
+    const OctArgs a = cloud_view(B, O, z);
+    const int p = p0 + (int)threadIdx.x;
+    if ((int)threadIdx.x < count)
+      finalize_slot(true, p, a, cloud_tags(O, z), a.prefix_n[0] / 3,
+                    s_nodes + threadIdx.x * kNodeWords);
+    bulk_fence_writes();
+    __syncthreads();
+    int* dst = reinterpret_cast<int*>(O.nodes + d.x);
+    const int words = count * kNodeWords;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0 && (words & 3) == 0) {
+      // one bulk copy of the staged block (the TMA engine writes it); done
+      // before the stage is reused
+      if (threadIdx.x == 0) {
+        bulk_store_s2g(dst, s_nodes, (uint32_t)words * 4u);
+        bulk_wait_all();
+      }
+      continue;
     }
-    return;
+    int k0 = 0;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+      const int quads = words >> 2;
+      const uint4* src4 = reinterpret_cast<const uint4*>(s_nodes);
+      uint4* dst4 = reinterpret_cast<uint4*>(dst);
+      for (int q = threadIdx.x; q < quads; q += kFinThreads) dst4[q] = src4[q];
+      k0 = quads << 2;
+    }
+    for (int q = k0 + threadIdx.x; q < words; q += kFinThreads) dst[q] = s_nodes[q];
   }
-  int k0 = 0;
-  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
-    const int quads = words >> 2;
-    const uint4* src4 = reinterpret_cast<const uint4*>(s_nodes);
-    uint4* dst4 = reinterpret_cast<uint4*>(dst);
-    for (int k = threadIdx.x; k < quads; k += kFinThreads) dst4[k] = src4[k];
-    k0 = quads << 2;
-  }
-  for (int k = k0 + threadIdx.x; k < words; k += kFinThreads) dst[k] = s_nodes[k];
 }
 
 __global__ void batch_publish_kernel(BatchDev B, BatchOctDev O, const uint32_t* status,
@@ -428,7 +453,7 @@ struct oct_batch_plan {
   size_t t_start = 0, t_node_start = 0, t_tile0 = 0, t_sort = 0, t_4k = 0, t_slots = 0,
          tables_bytes = 0;
   // workspace offsets
-  size_t w_status = 0, w_unique = 0, w_maxslot = 0, w_hist = 0,
+  size_t w_status = 0, w_queue = 0, w_unique = 0, w_maxslot = 0, w_hist = 0,
          zero_bytes = 0, w_tree = 0, w_base = 0, w_th = 0, w_keys_a = 0, w_keys_b = 0,
          w_tags = 0, ws_bytes = 0;
 };
@@ -436,6 +461,22 @@ struct oct_batch_plan {
 namespace {
 
 using octgb::align_up;
+
+// Batched tile kernels take their tiles from an atomic work queue (persistent
+// CTAs) unless switched to one CTA per tile.
+bool g_batch_queue = true;
+
+// Grid of a batched tile kernel: one CTA per tile without a queue; with one,
+// as many CTAs as fit on the device at once (no more than the tiles).
+template <typename K>
+int queue_grid(K kernel, int threads, int tiles, const uint32_t* queue) {
+  if (!queue) return std::max(tiles, 1);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return std::max(1, std::min(tiles, per_sm * octgb::device_sm_count()));
+}
 
 int batch_fail(cudaError_t e, const char* where) {
   char msg[192];
@@ -529,6 +570,7 @@ OCT_API oct_batch_plan* oct_batch_plan_create(int n_clouds, const int32_t* h_siz
   const int passes = P->sp.passes, bins = P->sp.bins;
   o = 0;
   P->w_status = take(4);
+  P->w_queue = take(64);  // work-queue counters: prefix sum, emit, finalize
   P->w_unique = take(4 * (size_t)n_clouds);
   P->w_maxslot = take(4 * (size_t)n_clouds);
   P->w_hist = take(4 * (size_t)n_clouds * passes * bins);
@@ -695,8 +737,9 @@ int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* p
     if (e == cudaSuccess) e = launch_tile_sums_scan(B.T4, TS.tile_sum, TS.tile_prefix, s);
     if (e != cudaSuccess) return batch_fail(e, "batch: tree");
     const OctTags tags = oct_tags_carve(w + P->w_tags, std::max(P->total_cap, 1));
-    batch_prefix_sum_kernel<<<B.T4, 256, 0, s>>>(B, unique_c, out->edge_count, out->prefix_sum,
-                                                 max_slot_c, TS.tile_prefix, tags);
+    uint32_t* queue = g_batch_queue ? reinterpret_cast<uint32_t*>(w + P->w_queue) : nullptr;
+    batch_prefix_sum_kernel<<<queue_grid(batch_prefix_sum_kernel, 256, B.T4, queue), 256, 0, s>>>(
+        B, unique_c, out->edge_count, out->prefix_sum, max_slot_c, TS.tile_prefix, tags, queue);
     BatchOctDev O;
     O.nodes = out->nodes;
     O.offsets = out->prefix_sum;
@@ -710,8 +753,11 @@ int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* p
     O.unique_c = unique_c;
     O.max_slot_c = max_slot_c;
     O.tags = tags;
-    batch_oct_emit_kernel<<<B.T4, 256, 0, s>>>(B, O, status);
-    if (B.Tn > 0) batch_oct_finalize_kernel<<<B.Tn, kFinThreads, 0, s>>>(B, O);
+    batch_oct_emit_kernel<<<queue_grid(batch_oct_emit_kernel, 256, B.T4, queue), 256, 0, s>>>(
+        B, O, status, queue ? queue + 4 : nullptr);
+    if (B.Tn > 0)
+      batch_oct_finalize_kernel<<<queue_grid(batch_oct_finalize_kernel, kFinThreads, B.Tn, queue),
+                                  kFinThreads, 0, s>>>(B, O, queue ? queue + 8 : nullptr);
     batch_publish_kernel<<<(P->C + 255) / 256, 256, 0, s>>>(B, O, status, d_cloud_counts);
   } else {
     e = cudaMemsetAsync(d_cloud_counts, 0, 16 * (size_t)P->C, s);
@@ -733,6 +779,12 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* P, const void* d_tables
                                    size_t workspace_bytes, oct_stream_t stream) {
   return batch_build(P, d_tables, points, d_mins, d_ranges, out, d_cloud_counts, workspace,
                      workspace_bytes, stream, nullptr);
+}
+
+OCT_API int oct_set_batch_work_queue(int on) {
+  if (on != 0 && on != 1) return OCT_ERR_INVALID_ARG;
+  g_batch_queue = on == 1;
+  return OCT_OK;
 }
 
 OCT_API size_t oct_batch_learned_workspace_bytes(const oct_batch_plan* P, int n_buckets) {

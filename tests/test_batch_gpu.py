@@ -118,3 +118,26 @@ def test_batch_512_clouds_match_single_builds():
         assert (got["n_unique"], got["n_oct"]) == (want["n_unique"], want["n_oct"]), c
         for key in STAGES:
             assert got[key].tobytes() == np.asarray(want[key]).tobytes(), (c, key)
+
+
+def test_work_queue_and_static_tiles_give_the_same_batch():
+    """The batched octree-stage kernels run from an atomic work queue
+    (persistent CTAs) or one CTA per tile; both equal the oracle."""
+    from pipeline_gb300 import _lib
+
+    lib = _lib.load()
+    clouds, mins, ranges = mixed_clouds(seed=4)
+    results = []
+    try:
+        for on in (0, 1):
+            assert lib.oct_set_batch_work_queue(on) == _lib.OCT_OK
+            b, pts, mn, rg = build_batch(clouds, mins, ranges)
+            b.build(pts, mn, rg)
+            results.append(b)
+    finally:
+        lib.oct_set_batch_work_queue(1)
+    assert results[0].same_results(results[1])
+    counts = results[1].cloud_counts()
+    for c in range(0, len(clouds), 3):
+        check_cloud(results[1], counts, c, clouds[c], mins[c], ranges[c])
+    assert lib.oct_set_batch_work_queue(2) == _lib.OCT_ERR_INVALID_ARG
