@@ -396,9 +396,10 @@ OCT_API int oct_build_octree_batch(const oct_batch_plan* plan, const void* d_tab
                                    size_t workspace_bytes, oct_stream_t stream);
 
 /* Scheduling of the batched build's octree-stage kernels (prefix sum, emit,
- * finalize): 1 (default) persistent CTAs take their tiles from an atomic work
- * queue; 0 one CTA per tile by block index. Results are the same; for
- * measurement. Applies to later builds in this process. */
+ * finalize): 1 persistent CTAs take their tiles from an atomic work queue;
+ * 0 (default) one CTA per tile by block index (the tiles are of equal size:
+ * the queue measured 0.99x on the 512-cloud batch). Results are the same.
+ * Applies to later builds in this process. */
 OCT_API int oct_set_batch_work_queue(int on);
 
 /* Learned + batched build (no counterpart in the reference): the batched

@@ -462,9 +462,10 @@ namespace {
 
 using octgb::align_up;
 
-// Batched tile kernels take their tiles from an atomic work queue (persistent
-// CTAs) unless switched to one CTA per tile.
-bool g_batch_queue = true;
+// Batched octree-stage kernels run one CTA per tile (the default: their
+// tiles are of equal size, and measured faster) or, when switched on, as
+// persistent CTAs taking tiles from an atomic work queue.
+bool g_batch_queue = false;
 
 // Grid of a batched tile kernel: one CTA per tile without a queue; with one,
 // as many CTAs as fit on the device at once (no more than the tiles).

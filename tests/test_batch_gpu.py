@@ -135,7 +135,7 @@ def test_work_queue_and_static_tiles_give_the_same_batch():
             b.build(pts, mn, rg)
             results.append(b)
     finally:
-        lib.oct_set_batch_work_queue(1)
+        lib.oct_set_batch_work_queue(0)
     assert results[0].same_results(results[1])
     counts = results[1].cloud_counts()
     for c in range(0, len(clouds), 3):
