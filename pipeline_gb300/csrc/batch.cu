@@ -286,14 +286,7 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   const int ns = B.node_start[c];
   const int hi = min(s_hi, B.node_start[c + 1] - ns - 1);
-  uint4* c4 = reinterpret_cast<uint4*>(tags.child);
-  for (int p = (int)ex + tid; p <= hi; p += 256) {
-    const size_t g = (size_t)ns + p;
-    c4[2 * g] = make_uint4(0, 0, 0, 0);
-    c4[2 * g + 1] = make_uint4(0, 0, 0, 0);
-    tags.owner[g] = 0;
-    tags.mask[g] = 0;
-  }
+  if (hi >= (int)ex) clear_tag_range(tags, (size_t)ns + ex, (size_t)ns + hi, tid, 256);
   }
 }
 

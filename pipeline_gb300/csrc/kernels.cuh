@@ -238,6 +238,21 @@ struct OctTags {
 size_t oct_tags_bytes(int cap);
 OctTags oct_tags_carve(void* base, int cap);
 
+// Zeroes the tags of slots [lo, hi] (inclusive) with `nthreads` threads of
+// index `tid`: consecutive threads take consecutive 16-byte child words, so
+// every warp store fills whole sectors.
+__device__ __forceinline__ void clear_tag_range(const OctTags& t, size_t lo, size_t hi, int tid,
+                                                int nthreads) {
+  if (hi < lo) return;
+  uint4* c4 = reinterpret_cast<uint4*>(t.child);
+  for (size_t q = 2 * lo + (size_t)tid; q < 2 * hi + 2; q += (size_t)nthreads)
+    c4[q] = make_uint4(0, 0, 0, 0);
+  for (size_t p = lo + (size_t)tid; p <= hi; p += (size_t)nthreads) {
+    t.owner[p] = 0;
+    t.mask[p] = 0;
+  }
+}
+
 enum OctMode { kOctMake = 1, kOctLink = 2, kOctFresh = 4 };
 
 struct OctArgs {

@@ -52,14 +52,9 @@ __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
     if (blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, kStatusCapacity);
     return;
   }
-  const int stride = gridDim.x * blockDim.x;
-  uint4* c4 = reinterpret_cast<uint4*>(t.child);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < z.n_oct; p += stride) {
-    c4[2 * p] = make_uint4(0, 0, 0, 0);
-    c4[2 * p + 1] = make_uint4(0, 0, 0, 0);
-    t.owner[p] = 0;
-    t.mask[p] = 0;
-  }
+  if (z.n_oct > 0)
+    clear_tag_range(t, 0, (size_t)z.n_oct - 1, blockIdx.x * blockDim.x + threadIdx.x,
+                    gridDim.x * blockDim.x);
 }
 
 __global__ void __launch_bounds__(256, 8) oct_emit_kernel(int mode, OctArgs a, OctTags t,

@@ -337,13 +337,7 @@ __global__ void __launch_bounds__(kEsThreads)
     __syncthreads();
     const int lo = (int)s_misc[3];
     const int hi = min(s_hi, zt.cap - 1);
-    uint4* c4 = reinterpret_cast<uint4*>(zt.child);
-    for (int p = lo + tid; p <= hi; p += kEsThreads) {
-      c4[2 * p] = make_uint4(0, 0, 0, 0);
-      c4[2 * p + 1] = make_uint4(0, 0, 0, 0);
-      zt.owner[p] = 0;
-      zt.mask[p] = 0;
-    }
+    if (hi >= lo) clear_tag_range(zt, (size_t)lo, (size_t)hi, tid, kEsThreads);
   }
   (void)tiles;
 }
