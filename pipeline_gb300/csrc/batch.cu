@@ -76,10 +76,14 @@ __global__ void __launch_bounds__(256)
     batch_morton_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, BatchDev B,
                         uint32_t* __restrict__ ghist, int passes, uint32_t* __restrict__ status) {
   constexpr int BINS = 1 << RB;
-  extern __shared__ uint32_t s_hist[];
+  constexpr int PASSES = (30 + RB - 1) / RB;  // the plan's passes over 30-bit codes
+  extern __shared__ uint32_t s_hist[];  // [PASSES * BINS] histograms, then the spread table
+  uint32_t* lut = s_hist + PASSES * BINS;
+  (void)passes;
   const int t0 = (int)((long long)B.Ts * blockIdx.x / gridDim.x);
   const int t1 = (int)((long long)B.Ts * (blockIdx.x + 1) / gridDim.x);
-  for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x) s_hist[i] = 0;
+  for (int i = threadIdx.x; i < PASSES * BINS; i += blockDim.x) s_hist[i] = 0;
+  fill_spread_lut(lut);
   __syncthreads();
   bool bad = false;
   int cur = t0 < t1 ? B.sort_tiles[t0].z : -1;
@@ -87,8 +91,8 @@ __global__ void __launch_bounds__(256)
     const int4 d = B.sort_tiles[t];
     if (d.z != cur) {  // flush the previous cloud's histograms
       __syncthreads();
-      uint32_t* g = ghist + (size_t)cur * passes * BINS;
-      for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x) {
+      uint32_t* g = ghist + (size_t)cur * PASSES * BINS;
+      for (int i = threadIdx.x; i < PASSES * BINS; i += blockDim.x) {
         if (s_hist[i]) atomicAdd(&g[i], s_hist[i]);
         s_hist[i] = 0;
       }
@@ -96,6 +100,7 @@ __global__ void __launch_bounds__(256)
       cur = d.z;
     }
     const float mn = B.mins[d.z], rg = B.ranges[d.z];
+    const float scale = __fdiv_rn(1024.0f, rg);
     // four loads in flight per thread, then the tile's tail
     constexpr int U = 4;
     int i = d.x + (int)threadIdx.x;
@@ -106,20 +111,22 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         bool ok;
-        const uint32_t c = morton_code(p[u].x, p[u].y, p[u].z, mn, rg, ok);
+        const uint32_t c = morton_code_lut(p[u].x, p[u].y, p[u].z, mn, rg, scale, lut, ok);
         bad |= !ok;
         keys[i + u * blockDim.x] = c;
-        for (int ps = 0; ps < passes; ++ps)
+#pragma unroll
+        for (int ps = 0; ps < PASSES; ++ps)
           atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);
       }
     }
     for (; i < d.y; i += blockDim.x) {
       const float4 p = ld_stream_f4(pts + i);
       bool ok;
-      const uint32_t c = morton_code(p.x, p.y, p.z, mn, rg, ok);
+      const uint32_t c = morton_code_lut(p.x, p.y, p.z, mn, rg, scale, lut, ok);
       bad |= !ok;
       keys[i] = c;
-      for (int ps = 0; ps < passes; ++ps)
+#pragma unroll
+      for (int ps = 0; ps < PASSES; ++ps)
         atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);
     }
   }
@@ -671,7 +678,8 @@ int batch_build(const oct_batch_plan* P, const void* d_tables, const oct_vec4* p
   }
   if (P->N > 0) {
     const int mgrid = std::max(1, std::min(B.Ts, sms * 16));
-    const size_t msm = 4 * (size_t)passes * bins;
+    const size_t msm = 4 * ((size_t)passes * bins + 1024);  // histograms + spread table
+    if (passes != (30 + rb - 1) / rb) return OCT_ERR_INVALID_ARG;
     if (rb == 10) {
       batch_morton_kernel<10><<<mgrid, 256, msm, s>>>(reinterpret_cast<const float4*>(points), ka,
                                                       B, hist, passes, status);

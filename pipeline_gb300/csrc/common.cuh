@@ -205,6 +205,22 @@ __device__ __forceinline__ uint32_t morton_code(float x, float y, float z, float
   return spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
 }
 
+// The same code with the bit spreads read from a table in shared memory
+// (lut[v] = spread3(v), v < 1024: fill_spread_lut) and the 1024 / range
+// quotient computed by the caller (scale = __fdiv_rn(1024.0f, range)).
+__device__ __forceinline__ void fill_spread_lut(uint32_t* lut) {
+  for (uint32_t v = threadIdx.x; v < 1024u; v += blockDim.x) lut[v] = spread3(v);
+}
+__device__ __forceinline__ uint32_t morton_code_lut(float x, float y, float z, float min_coord,
+                                                    float range, float scale,
+                                                    const uint32_t* lut, bool& ok) {
+  ok = true;
+  const uint32_t qx = quantise(x, min_coord, range, scale, ok);
+  const uint32_t qy = quantise(y, min_coord, range, scale, ok);
+  const uint32_t qz = quantise(z, min_coord, range, scale, ok);
+  return lut[qx & 0x3ffu] | (lut[qy & 0x3ffu] << 1) | (lut[qz & 0x3ffu] << 2);
+}
+
 // morton32_to_xyz: per axis (raw / 1024) * range + min, w = 1.
 __device__ __forceinline__ float4 decode_corner(uint32_t code, float min_coord, float range) {
   float4 c;

@@ -32,11 +32,15 @@ __global__ void __launch_bounds__(256)
                   float min_coord, float range, uint32_t* __restrict__ ghist, int passes,
                   uint32_t* __restrict__ status) {
   constexpr int BINS = 1 << RB;
-  extern __shared__ uint32_t s_hist[];
-  if (HIST) {
-    for (int i = threadIdx.x; i < passes * BINS; i += blockDim.x) s_hist[i] = 0;
-    __syncthreads();
-  }
+  constexpr int PASSES = (30 + RB - 1) / RB;  // the plan's passes over 30-bit codes
+  extern __shared__ uint32_t s_hist[];  // [PASSES * BINS] histograms, then the spread table
+  uint32_t* lut = s_hist + (HIST ? PASSES * BINS : 0);
+  if (HIST)
+    for (int i = threadIdx.x; i < PASSES * BINS; i += blockDim.x) s_hist[i] = 0;
+  fill_spread_lut(lut);
+  __syncthreads();
+  (void)passes;
+  const float scale = __fdiv_rn(1024.0f, range);
   bool bad = false;
   const long long stride = (long long)gridDim.x * blockDim.x;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,27 +52,31 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       bool ok;
-      const uint32_t c = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range, ok);
+      const uint32_t c = morton_code_lut(p[u].x, p[u].y, p[u].z, min_coord, range, scale, lut, ok);
       bad |= !ok;
       keys[i + u * stride] = c;
-      if (HIST)
-        for (int ps = 0; ps < passes; ++ps)
+      if (HIST) {
+#pragma unroll
+        for (int ps = 0; ps < PASSES; ++ps)
           atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);
+      }
     }
   }
   for (; i < n; i += stride) {
     const float4 p = ld_stream_f4(pts + i);
     bool ok;
-    const uint32_t c = morton_code(p.x, p.y, p.z, min_coord, range, ok);
+    const uint32_t c = morton_code_lut(p.x, p.y, p.z, min_coord, range, scale, lut, ok);
     bad |= !ok;
     keys[i] = c;
-    if (HIST)
-      for (int ps = 0; ps < passes; ++ps)
+    if (HIST) {
+#pragma unroll
+      for (int ps = 0; ps < PASSES; ++ps)
         atomicAdd(&s_hist[ps * BINS + ((c >> (ps * RB)) & (BINS - 1))], 1u);
+    }
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) raise_status(status, kStatusRange);
   if (HIST) {
-    for (int b = threadIdx.x; b < passes * BINS; b += blockDim.x)
+    for (int b = threadIdx.x; b < PASSES * BINS; b += blockDim.x)
       if (s_hist[b]) atomicAdd(&ghist[b], s_hist[b]);
   }
 }
@@ -674,8 +682,9 @@ cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float 
   long long need = (n + 255) / 256;
   const int grid = (int)(need < blocks ? need : blocks);
   if (plan) {
+    if (plan->passes != (30 + plan->radix_bits - 1) / plan->radix_bits) return cudaErrorInvalidValue;
     uint32_t* hist = reinterpret_cast<uint32_t*>(static_cast<char*>(ctrl) + plan->hist_off);
-    const size_t sm = sizeof(uint32_t) * plan->passes * plan->bins;
+    const size_t sm = sizeof(uint32_t) * (plan->passes * plan->bins + 1024);
     if (plan->radix_bits == 10)
       morton_kernel<10, true><<<grid, 256, sm, s>>>(pts, keys, n, min_coord, range, hist,
                                                     plan->passes, status);
@@ -683,8 +692,8 @@ cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float 
       morton_kernel<8, true><<<grid, 256, sm, s>>>(pts, keys, n, min_coord, range, hist,
                                                    plan->passes, status);
   } else {
-    morton_kernel<10, false><<<grid, 256, 0, s>>>(pts, keys, n, min_coord, range, nullptr, 0,
-                                                  status);
+    morton_kernel<10, false><<<grid, 256, sizeof(uint32_t) * 1024, s>>>(pts, keys, n, min_coord,
+                                                                        range, nullptr, 0, status);
   }
   return cudaGetLastError();
 }
