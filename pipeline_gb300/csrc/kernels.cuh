@@ -79,15 +79,18 @@ SortPlan sort_plan(int n, int key_bits);
 SortPlan sort_plan_cfg(int n, int key_bits, SortConfig cfg);
 // One digit pass (batched sorts: tile descriptors int4{first, end, cloud,
 // first tile of cloud} and their count; nullptr / 0 for a single array).
-// A launch that serves as either of two passes, chosen on the device: when
-// *flag != 0 the tile histogram, tile scan and pass kernels use this shift,
-// these digit bases and these split sums instead of their own.
+// A pass launch that serves as either of two passes, chosen on the device:
+// when *flag != 0 the pass kernel uses this shift and these digit bases, and
+// an unstable reduce-then-scan pass takes its digit runs' places from the
+// cursors in `part` (one per digit, kCursorStride words apart, zeroed before
+// the sort) instead of the tile scan.
 struct DigitAlt {
   const uint32_t* flag = nullptr;
   int shift = 0;
   const uint32_t* base = nullptr;
   uint32_t* part = nullptr;
 };
+constexpr int kCursorStride = 16;
 cudaError_t launch_pass(const SortPlan& p, bool stable, const uint32_t* src, uint32_t* dst,
                         int shift, const uint32_t* base, uint32_t* lookback, uint32_t* counter,
                         const uint32_t* tile_prefix, uint32_t* status, const uint32_t* gate,

@@ -252,9 +252,14 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
                      const uint32_t* __restrict__ gate, const int4* __restrict__ tdesc,
                      DigitAlt alt) {
   if (gate && *gate == 0) return;
+  // The MSD form's top-digit scatter: the order inside a bucket is free, so a
+  // tile takes its digit runs' places with one atomic add per digit on the
+  // bucket's cursor (alt.part, 16 words apart) instead of the tile scan.
+  bool cursors = false;
   if (alt.flag && *alt.flag) {
     shift = alt.shift;
     bin_base = alt.base;
+    cursors = !STABLE && SCAN == 1;
   }
   using L = PassSmem<RB, WARPS, ITEMS, STABLE>;
   constexpr int BINS = L::BINS, THREADS = WARPS * 32, TILE = L::TILE;
@@ -356,6 +361,9 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
     bin_local[b] = run;
     if (SCAN == 0)
       st_relaxed_u32(lookback + (size_t)tile * BINS + b, (tile == 0 ? kFlagInc : kFlagAgg) | own[j]);
+    if (SCAN == 1 && cursors)
+      bin_glob[b] = bin_base[b] + (own[j] ? atomicAdd(alt.part + (size_t)b * kCursorStride, own[j])
+                                          : 0u);
   }
   __syncthreads();
 
@@ -381,8 +389,12 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
   __syncthreads();
 
   if (SCAN == 1) {
-    for (int b = tid; b < BINS; b += THREADS)
-      bin_glob[b] = tile_prefix[(size_t)tile * BINS + b] - bin_local[b];
+    if (cursors) {
+      for (int b = tid; b < BINS; b += THREADS) bin_glob[b] -= bin_local[b];
+    } else {
+      for (int b = tid; b < BINS; b += THREADS)
+        bin_glob[b] = tile_prefix[(size_t)tile * BINS + b] - bin_local[b];
+    }
   } else {
     // Decoupled look-back per digit (digit_lookback).
 #pragma unroll
@@ -428,6 +440,8 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
 // splits; tile_hist also adds each tile's counts into its split's partial
 // sums, so the tile scan runs every split in its own CTAs.
 constexpr int kScanSplits = 16;
+// the MSD form's bucket cursors live in the top digit's split sums
+static_assert(kCursorStride <= kScanSplits, "one cursor per digit in the split sums");
 
 __host__ __device__ __forceinline__ int split_tiles(int tiles) {
   return (tiles + kScanSplits - 1) / kScanSplits;
@@ -437,13 +451,8 @@ template <int RB>
 __global__ void __launch_bounds__(256)
     tile_hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tile_keys,
                      uint32_t* __restrict__ th, const uint32_t* __restrict__ gate,
-                     const int4* __restrict__ tdesc, uint32_t* __restrict__ part, int tiles,
-                     DigitAlt alt) {
+                     const int4* __restrict__ tdesc, uint32_t* __restrict__ part, int tiles) {
   if (gate && *gate == 0) return;
-  if (alt.flag && *alt.flag) {
-    shift = alt.shift;
-    part = alt.part;
-  }
   constexpr int BINS = 1 << RB;
   __shared__ uint32_t h[BINS];
   // CTAs walk the tiles (a capped grid: a gated-off launch schedules few CTAs)
@@ -490,12 +499,8 @@ static int tile_hist_grid(int tiles) {
 __global__ void __launch_bounds__(1024)
     tile_scan_split_kernel(uint32_t* __restrict__ th, int tiles, int bins,
                            const uint32_t* __restrict__ bin_base, const uint32_t* __restrict__ part,
-                           const uint32_t* __restrict__ gate, DigitAlt alt) {
+                           const uint32_t* __restrict__ gate) {
   if (gate && *gate == 0) return;
-  if (alt.flag && *alt.flag) {
-    bin_base = alt.base;
-    part = alt.part;
-  }
   __shared__ uint32_t sums[32][33];
   const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + l;
@@ -739,9 +744,10 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(rec, s);
-  // The MSD form's top-digit scatter reuses pass 0's launches (unstable, the
-  // top digit's shift, bases and split sums, chosen on the device); the later
-  // passes then return at once.
+  // The MSD form's top-digit scatter reuses pass 0's pass launch (unstable,
+  // the top digit's shift and bases, its places from bucket cursors kept in
+  // the top digit's zeroed split sums, chosen on the device); the later passes
+  // then return at once.
   DigitAlt alt0;
   if (msd_flag && msd_plan_ok(*plan)) {
     const int top = plan->passes - 1;
@@ -757,15 +763,18 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
     const uint32_t* g = (p > 0 && lsd_flag) ? lsd_flag : gate;
     const DigitAlt da = p == 0 ? alt0 : DigitAlt{};
     if (plan->cfg.scan == 1) {
+      // the MSD form's scatter takes its places from the bucket cursors: the
+      // tile histograms and their scan run for the LSD form only
+      const uint32_t* gs = (p == 0 && alt0.flag) ? lsd_flag : g;
       uint32_t* pp = part + (size_t)p * kScanSplits * plan->bins;
       if (plan->radix_bits == 10)
-        tile_hist_kernel<10><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
-                                                         nullptr, pp, plan->tiles, da);
+        tile_hist_kernel<10><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gs,
+                                                         nullptr, pp, plan->tiles);
       else
-        tile_hist_kernel<8><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, g,
-                                                        nullptr, pp, plan->tiles, da);
+        tile_hist_kernel<8><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gs,
+                                                        nullptr, pp, plan->tiles);
       tile_scan_split_kernel<<<dim3((plan->bins + 31) / 32, kScanSplits), 1024, 0, s>>>(
-          th, plan->tiles, plan->bins, base + p * plan->bins, pp, g, da);
+          th, plan->tiles, plan->bins, base + p * plan->bins, pp, gs);
     }
     uint32_t* lb = lookback + (size_t)p * plan->tiles * plan->bins;
     e = launch_pass(*plan, p > 0, a, b, shift, base + p * plan->bins,
@@ -811,11 +820,9 @@ cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int sh
   // a gated launch walks the tiles from a capped grid (few no-op CTAs)
   const int grid = gate ? tile_hist_grid(tiles) : tiles;
   if (radix_bits == 10)
-    tile_hist_kernel<10><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles,
-                                              DigitAlt{});
+    tile_hist_kernel<10><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles);
   else
-    tile_hist_kernel<8><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles,
-                                             DigitAlt{});
+    tile_hist_kernel<8><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles);
   return cudaGetLastError();
 }
 
