@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(256, 8) oct_emit_kernel(int mode, OctArgs a, O
     emit_node(mode, i, a, t, z, status);
 }
 
-__global__ void __launch_bounds__(kFinThreads, 6) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
+__global__ void __launch_bounds__(kFinThreads, 8) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
   __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
   const Sizes z = read_sizes(a);
   if (!z.fits || z.n_brt < 1) return;
