@@ -517,6 +517,13 @@ def profile_only(args):
         k_ComputeMortonCode(pts.index_select(0, idx).contiguous(), sk, s_n, MIN_COORD, RANGE)
         model = LearnedCDF(max_segments=4096).fit(sk, n_segments=4096, steps=0, n_buckets=4096)
         b = LearnedOctreeBuilder(n, model)
+    elif args.profile_only == "clustered":
+        # plain build of the clustered cloud of n points (uneven top digits:
+        # stages 2-3 take the LSD form)
+        from pipeline_gb300 import datasets
+
+        pts = torch.from_numpy(datasets.clustered(n, seed=7)).cuda()
+        b = OctreeBuilder(n)
     else:
         pts = torch.from_numpy(make_points(n)).cuda()
         b = OctreeBuilder(n)
@@ -971,7 +978,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the clustered (learned) and batched workloads")
     ap.add_argument("--profile-only", nargs="?", const="plain",
-                    choices=["plain", "learned", "batched"],
+                    choices=["plain", "learned", "clustered", "batched"],
                     help="warm-up builds plus one build, no timing or output (for ncu captures)")
     ap.add_argument("--shard", choices=["batched"], default=None,
                     help="split the 512-cloud batched workload over the ranks (one line)")

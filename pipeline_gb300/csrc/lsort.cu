@@ -4,11 +4,12 @@
 // scatter into buckets followed by an independent sort of each bucket, and the
 // unique pass fuses into the bucket stage (equal keys share a bucket):
 //
-//   hist     per-chunk bucket counts (Morton fused when starting from points)
-//   offsets  per-bucket totals and per-chunk offsets; bucket starts; overflow
-//            fraction (keys in buckets above the bitonic capacity) and the
-//            fallback decision when it exceeds the threshold
-//   scatter  each chunk writes its keys into its reserved bucket ranges
+//   bin      one pass over the points (or keys): Morton code, bucket, and a
+//            place in the bucket's fixed range of cap keys, reserved per
+//            tile and bucket on the bucket's cursor (see the bin section)
+//   stats    bucket counts from the cursors; overflow fraction (keys in
+//            buckets above the bitonic capacity) and the fallback decision
+//            (a bucket past cap, or the fraction above the threshold)
 //   buckets  one CTA per bucket: the sorted unique keys of the bucket from a
 //            shared-memory bitmap over [min, max] of its keys when that is
 //            dense enough, else a radix sort (or, above the cache size, a
@@ -37,8 +38,6 @@
 
 namespace octgb {
 
-constexpr int kLsThreads = 1024;          // histogram / scatter CTAs (2 per SM)
-constexpr int kLsUnroll = 4;              // keys per thread in flight
 constexpr int kBkThreads = 512;           // bucket CTAs (3 per SM)
 constexpr int kBkWarps = kBkThreads / 32;
 constexpr int kBkWords = 16384;           // 64 KiB working region per bucket CTA
@@ -52,8 +51,9 @@ constexpr int kRsBins = 1 << kRsBits;
 
 // ------------------------------------------------------- bucket lookup --
 struct BucketLookup {
-  const uint32_t* bounds;  // [nb] smallest key of each bucket
-  const uint16_t* blut;    // [2^14 + 1] bucket at the start of each 2^16-key cell
+  const uint32_t* bounds;  // [nb] smallest key of each bucket (shared memory)
+  const uint16_t* blut;    // [2^14 + 1] bucket at the start of each 2^16-key cell (shared,
+                           // 4-byte aligned)
   uint32_t last;           // nb - 1
 };
 
@@ -87,126 +87,186 @@ __device__ __forceinline__ uint32_t bucket_of(const BucketLookup& q, uint32_t v)
   return lo;
 }
 
+// Shared memory of the batched histogram and scatter kernels: counts or
+// cursors [nb], bounds [nb], the bucket table [2^14 + 1].
 size_t lsort_hist_smem(int nb, int /*max_segments*/) {
-  return align_up(8 * (size_t)nb + 2 * ((size_t)kLcdfBlutSize + 1), 16);
+  return align_up(8 * (size_t)nb + 2 * ((size_t)kLcdfBlutSize + 2), 16);
 }
 
-// ------------------------------------------------------------- histogram --
+// ------------------------------------------------------------------- bin --
+// One pass over the points (or keys) does what a histogram pass and a
+// scatter pass would: the Morton code, its bucket and its place in the
+// bucket. Bucket b owns the fixed range [b * cap, (b + 1) * cap) of bkeys.
+// CTAs (one per SM) walk tiles of up to kBinTile keys (1,024 x items, items
+// chosen so that small clouds still spread over the SMs): shared-memory atomics rank a
+// tile's keys per bucket, one atomicAdd on the bucket's cursor reserves each
+// bucket's run, the keys are staged in bucket order and leave bucket by
+// bucket, so the runs that consecutive tiles write into a bucket lie next to
+// each other. A bucket that outgrows cap drops the keys past it; its cursor
+// still counts them, which sends the sort to the fallback.
+constexpr int kBinThreads = 1024;
+constexpr int kBinItems = 8;
+constexpr int kBinTile = kBinThreads * kBinItems;  // 8,192 keys
+static_assert(kBinTile <= 32768, "ranks are kept in 15 bits");
+
+// counts, local starts, run bases and bounds [nb] each, the Morton spread
+// table [1024], the staged keys [kBinTile] and their buckets, the bucket table
+size_t lsort_bin_smem(int nb) {
+  return align_up(16 * (size_t)nb + 4 * 1024 + 6 * (size_t)kBinTile +
+                      2 * ((size_t)kLcdfBlutSize + 2),
+                  16);
+}
+
 template <bool FROM_POINTS>
-__global__ void __launch_bounds__(kLsThreads, 2)
-    lsort_hist_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, int n,
-                      float min_coord, float range, const char* __restrict__ blob, LcdfLayout L,
-                      uint32_t* __restrict__ chunk_hist, int nb, uint32_t* __restrict__ status) {
+__global__ void __launch_bounds__(kBinThreads, 1)
+    lsort_bin_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, int n,
+                     float min_coord, float range, const char* __restrict__ blob, LcdfLayout L,
+                     int nb, uint32_t cap, int items, uint32_t* __restrict__ cursor,
+                     uint32_t* __restrict__ bkeys, uint32_t* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char sm[];
-  uint32_t* s_hist = reinterpret_cast<uint32_t*>(sm);
-  for (int b = threadIdx.x; b < nb; b += kLsThreads) s_hist[b] = 0;
-  const BucketLookup q = load_lookup(blob, L, nb, s_hist + nb,
-                                     reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
-  const int G = gridDim.x, c = blockIdx.x;
-  const int lo = (int)((long long)n * c / G), hi = (int)((long long)n * (c + 1) / G);
-  bool bad = false;
-  constexpr int U = FROM_POINTS ? 2 : kLsUnroll;  // float4 points: 2 in flight fit 32 registers
-  for (int base = lo + threadIdx.x; base < hi; base += U * kLsThreads) {
-    uint32_t code[U];
-    if (FROM_POINTS) {
-      float4 p[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * kLsThreads;
-        if (i < hi) p[u] = ld_stream_f4(pts + i);
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * kLsThreads;
-        if (i < hi) {
-          bool ok;
-          code[u] = morton_code(p[u].x, p[u].y, p[u].z, min_coord, range, ok);
-          bad |= !ok;
-          keys[i] = code[u];
-        }
-      }
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * kLsThreads;
-        if (i < hi) code[u] = keys[i];
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (base + u * kLsThreads < hi) atomicAdd(&s_hist[bucket_of(q, code[u])], 1u);
-  }
-  if (FROM_POINTS && __syncthreads_or(bad) && threadIdx.x == 0) raise_status(status, kStatusRange);
-  __syncthreads();
-  uint32_t* row = chunk_hist + (size_t)c * nb;
-  for (int b = threadIdx.x; b < nb; b += kLsThreads) row[b] = s_hist[b];
-}
-
-// --------------------------------------------------------------- offsets --
-// Block: 32 buckets x 8 chunk groups. chunk_hist[c][b] becomes the exclusive
-// offset of chunk c inside bucket b; totals[b] the bucket's count.
-__global__ void __launch_bounds__(256)
-    lsort_offsets_kernel(uint32_t* __restrict__ chunk_hist, int G, int nb,
-                         uint32_t* __restrict__ totals) {
-  __shared__ uint32_t part[8][33];
-  const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int b = blockIdx.x * 32 + l;
-  const int c0 = (int)((long long)G * w / 8), c1 = (int)((long long)G * (w + 1) / 8);
-  uint32_t sum = 0;
-  if (b < nb)
-    for (int c = c0; c < c1; ++c) sum += chunk_hist[(size_t)c * nb + b];
-  part[w][l] = sum;
-  __syncthreads();
-  uint32_t base = 0;
-  for (int k = 0; k < w; ++k) base += part[k][l];
-  if (w == 7 && b < nb) totals[b] = base + sum;
-  if (b < nb) {
-    uint32_t run = base;
-    for (int c = c0; c < c1; ++c) {
-      const uint32_t v = chunk_hist[(size_t)c * nb + b];
-      chunk_hist[(size_t)c * nb + b] = run;
-      run += v;
-    }
-  }
-}
-
-// One block: bucket starts (exclusive scan of totals), overflow fraction and
-// the fallback decision (also taken when the model's tables do not match).
-__global__ void __launch_bounds__(1024)
-    lsort_scan_kernel(const uint32_t* __restrict__ totals, int nb, int n, float threshold,
-                      const char* __restrict__ blob, uint32_t* __restrict__ starts,
-                      LsortStats* __restrict__ stats) {
   __shared__ uint32_t warp_tot[32];
   __shared__ uint32_t total;
-  __shared__ uint32_t s_over, s_max;
+  uint32_t* s_cnt = reinterpret_cast<uint32_t*>(sm);
+  uint32_t* s_lstart = s_cnt + nb;
+  uint32_t* s_gbase = s_lstart + nb;
+  uint32_t* s_bounds = s_gbase + nb;
+  uint32_t* spread = s_bounds + nb;
+  uint32_t* st_key = spread + 1024;
+  uint16_t* st_bid = reinterpret_cast<uint16_t*>(st_key + kBinTile);
+  uint16_t* s_coarse = st_bid + kBinTile;
+  if (FROM_POINTS) fill_spread_lut(spread);
+  const BucketLookup q = load_lookup(blob, L, nb, s_bounds, s_coarse);
+  const float scale = __fdiv_rn(1024.0f, range);
+  const int tid = threadIdx.x;
+  const int tile = kBinThreads * items;  // items in [1, kBinItems]
+  const int tiles = (n + tile - 1) / tile;
+  const int per = (nb + kBinThreads - 1) / kBinThreads;  // buckets per thread in the scan
+  bool bad = false;
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+    for (int b = tid; b < nb; b += kBinThreads) s_cnt[b] = 0;
+    __syncthreads();
+    const int t0 = t * tile;
+    uint32_t code[kBinItems], br[kBinItems];  // code; bucket << 16 | rank in the bucket
+#pragma unroll
+    for (int h = 0; h < kBinItems; h += 4) {
+      float4 p[4];
+      uint32_t kk[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = t0 + (h + u) * kBinThreads + tid;
+        const bool in = h + u < items && i < n;
+        if (FROM_POINTS) {
+          if (in) p[u] = ld_stream_f4(pts + i);
+        } else {
+          kk[u] = in ? __ldcs(keys + i) : 0u;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = t0 + (h + u) * kBinThreads + tid;
+        code[h + u] = 0;
+        br[h + u] = 0;
+        if (h + u < items && i < n) {
+          uint32_t c;
+          if (FROM_POINTS) {
+            bool ok;
+            c = morton_code_lut(p[u].x, p[u].y, p[u].z, min_coord, range, scale, spread, ok);
+            bad |= !ok;
+            keys[i] = c;  // the fallback sorts these
+          } else {
+            c = kk[u];
+          }
+          code[h + u] = c;
+        }
+        // Only unique keys are needed: a key equal to the previous lane's
+        // (the key before it) stays out of the buckets, so runs of one cell
+        // (scan-ordered clouds) shrink before the buckets see them. Lanes
+        // hold consecutive keys and the valid ones are a prefix of the warp.
+        const uint32_t prev = __shfl_up_sync(0xffffffffu, code[h + u], 1);
+        if (h + u < items && i < n && ((tid & 31) == 0 || prev != code[h + u])) {
+          const uint32_t b = bucket_of(q, code[h + u]);
+          br[h + u] = (b << 16) | atomicAdd(&s_cnt[b], 1u) | 0x8000u;  // bit 15: placed
+        }
+      }
+    }
+    __syncthreads();
+    // Local starts (exclusive scan over buckets); each bucket's run reserved.
+    int placed;  // keys of the tile that go to buckets
+    {
+      const int b0 = tid * per, b1 = min(b0 + per, nb);
+      uint32_t sum = 0;
+      for (int b = b0; b < b1; ++b) sum += s_cnt[b];
+      uint32_t run = block_exclusive_sum<kBinThreads>(sum, warp_tot, &total);
+      placed = (int)total;
+      // four buckets at a time: their cursor atomics are in flight together
+      for (int b = b0; b < b1; b += 4) {
+        uint32_t c[4], g[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = b + k < b1 ? s_cnt[b + k] : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) g[k] = c[k] ? atomicAdd(cursor + b + k, c[k]) : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (b + k < b1) {
+            s_lstart[b + k] = run;
+            s_gbase[b + k] = g[k] - run;  // tile position j of the bucket goes to slot s_gbase + j
+            run += c[k];
+          }
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kBinItems; ++it) {
+      if (br[it] & 0x8000u) {
+        const uint32_t b = br[it] >> 16;
+        const uint32_t pos = s_lstart[b] + (br[it] & 0x7fffu);
+        st_key[pos] = code[it];
+        st_bid[pos] = (uint16_t)b;
+      }
+    }
+    __syncthreads();
+    for (int j = tid; j < placed; j += kBinThreads) {
+      const uint32_t b = st_bid[j];
+      const uint32_t o = s_gbase[b] + (uint32_t)j;
+      if (o < cap) bkeys[(size_t)b * cap + o] = st_key[j];
+    }
+    __syncthreads();  // the stage and counters are the next tile's
+  }
+  if (FROM_POINTS && __syncthreads_or(bad) && tid == 0) raise_status(status, kStatusRange);
+}
+
+// One block: bucket totals from the cursors, the fixed bucket starts
+// (b * cap), overflow fraction and the fallback decision (a bucket past cap,
+// too many keys in buckets above the bitonic capacity, or tables built for
+// another bucket count).
+__global__ void __launch_bounds__(1024)
+    lsort_bin_stats_kernel(const uint32_t* __restrict__ cursor, int nb, int n, uint32_t cap,
+                           float threshold, const char* __restrict__ blob,
+                           uint32_t* __restrict__ starts, uint32_t* __restrict__ counts,
+                           LsortStats* __restrict__ stats) {
+  __shared__ uint32_t s_over, s_max, s_spill;
   if (threadIdx.x == 0) {
     s_over = 0;
     s_max = 0;
+    s_spill = 0;
   }
   __syncthreads();
-  const int per = (nb + 1023) / 1024;
-  uint32_t sum = 0, over = 0, mx = 0;
-  for (int j = 0; j < per; ++j) {
-    const int b = threadIdx.x * per + j;
-    if (b < nb) {
-      const uint32_t v = totals[b];
-      sum += v;
-      if (v > (uint32_t)kCap) over += v;
-      mx = max(mx, v);
-    }
+  uint32_t over = 0, mx = 0, spill = 0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const uint32_t v = cursor[b];
+    if (v > (uint32_t)kCap) over += v;
+    if (v > cap) spill = 1u;
+    mx = max(mx, v);
+    starts[b] = (uint32_t)b * cap;
+    counts[b] = min(v, cap);
   }
   atomicAdd(&s_over, over);
   atomicMax(&s_max, mx);
-  uint32_t run = block_exclusive_sum<1024>(sum, warp_tot, &total);
-  for (int j = 0; j < per; ++j) {
-    const int b = threadIdx.x * per + j;
-    if (b < nb) {
-      starts[b] = run;
-      run += totals[b];
-    }
-  }
+  if (spill) atomicOr(&s_spill, 1u);
+  __syncthreads();
   if (threadIdx.x == 0) {
-    starts[nb] = total;
+    starts[nb] = (uint32_t)nb * cap;
     stats->overflow_keys = s_over;
     stats->max_bucket = s_max;
     stats->n = (uint32_t)n;
@@ -215,43 +275,9 @@ __global__ void __launch_bounds__(1024)
     const LcdfHeader* h = reinterpret_cast<const LcdfHeader*>(blob);
     const bool model_ok = h->magic == kLcdfMagic && h->version == kLcdfVersion &&
                           h->n_buckets == nb;
-    // Fallback when too many keys sit in oversized buckets (load imbalance)
-    // or when the bucket tables belong to another bucket count.
-    if (frac > threshold || !model_ok) {
+    if (frac > threshold || !model_ok || s_spill) {
       stats->skip = 1u;
       stats->fallback = 1u;
-    }
-  }
-}
-
-// --------------------------------------------------------------- scatter --
-__global__ void __launch_bounds__(kLsThreads, 2)
-    lsort_scatter_kernel(const uint32_t* __restrict__ keys, int n, const char* __restrict__ blob,
-                         LcdfLayout L, const uint32_t* __restrict__ chunk_off,
-                         const uint32_t* __restrict__ starts, int nb, uint32_t* __restrict__ out,
-                         const LsortStats* __restrict__ stats) {
-  if (stats->skip) return;
-  extern __shared__ __align__(16) unsigned char sm[];
-  uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
-  const int G = gridDim.x, c = blockIdx.x;
-  for (int b = threadIdx.x; b < nb; b += kLsThreads)
-    cursor[b] = starts[b] + chunk_off[(size_t)c * nb + b];
-  const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
-                                     reinterpret_cast<uint16_t*>(cursor + 2 * nb));
-  const int lo = (int)((long long)n * c / G), hi = (int)((long long)n * (c + 1) / G);
-  for (int base = lo + threadIdx.x; base < hi; base += kLsUnroll * kLsThreads) {
-    uint32_t k[kLsUnroll];
-#pragma unroll
-    for (int u = 0; u < kLsUnroll; ++u) {
-      const int i = base + u * kLsThreads;
-      if (i < hi) k[u] = keys[i];
-    }
-#pragma unroll
-    for (int u = 0; u < kLsUnroll; ++u) {
-      if (base + u * kLsThreads < hi) {
-        const uint32_t pos = atomicAdd(&cursor[bucket_of(q, k[u])], 1u);
-        if (pos < (uint32_t)n) out[pos] = k[u];
-      }
     }
   }
 }
@@ -444,19 +470,27 @@ __global__ void __launch_bounds__(kBkThreads, 3)
   const uint32_t span_m1 = cnt > 0 ? kmax - kmin : 0u;  // span - 1
 
   // 0: bitmap in the second half, keys cached in the first (output staged);
-  //    taken while the bitmap has at most 2 words per key (dense buckets)
-  // 1: bitmap over the whole region (keys re-read, output written directly)
+  //    taken while the bitmap has at most 4 words per key (dense buckets)
+  // 1: bitmap over the whole region (keys re-read, output written directly):
+  //    buckets above the cache size, or cached ones that are as dense but
+  //    span more than the second half
   // 2: sorted keys: radix sort of the cached keys (cnt <= kBkCache) or
   //    bitonic sort of up to kCap keys over the whole region
   // 3: neither fits
+  // Walking a bitmap word costs a few instructions where ranking a key costs
+  // tens per 8-bit pass (2-3 passes for these spans): up to 4 words per key
+  // the bitmap is cheaper.
   const uint32_t words_needed = (span_m1 >> 5) + 1u;
+  const bool dense = words_needed <= max(4u * (uint32_t)cnt, 256u);
   int path;
   bool radix = false;
   if (cnt == 0) {
     path = 0;
   } else if (cached) {
-    if (span_m1 < kBmSmall && words_needed <= max(2u * (uint32_t)cnt, 256u)) {
+    if (span_m1 < kBmSmall && dense) {
       path = 0;
+    } else if (span_m1 < kBmBig && dense) {
+      path = 1;
     } else {
       path = 2;
       radix = true;
@@ -635,8 +669,8 @@ __global__ void __launch_bounds__(256)
                    uint32_t* __restrict__ tile_off) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* s_hist = reinterpret_cast<uint32_t*>(sm);
-  const BucketLookup q = load_lookup(blob, L, nb, s_hist + nb,
-                                     reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
+  const BucketLookup q =
+      load_lookup(blob, L, nb, s_hist + nb, reinterpret_cast<uint16_t*>(s_hist + 2 * nb));
   const int lane = threadIdx.x & 31;
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     for (int b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0;
@@ -703,8 +737,8 @@ __global__ void __launch_bounds__(256)
                       LcdfLayout L, int nb, const uint32_t* __restrict__ tile_off) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* cursor = reinterpret_cast<uint32_t*>(sm);
-  const BucketLookup q = load_lookup(blob, L, nb, cursor + nb,
-                                     reinterpret_cast<uint16_t*>(cursor + 2 * nb));
+  const BucketLookup q =
+      load_lookup(blob, L, nb, cursor + nb, reinterpret_cast<uint16_t*>(cursor + 2 * nb));
   const int lane = threadIdx.x & 31;
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const uint32_t* row = tile_off + (size_t)t * nb;
@@ -819,7 +853,6 @@ LsortPlan lsort_plan(int n, int nb, int max_segments) {
   LsortPlan p{};
   p.n = n;
   p.nb = nb;
-  p.chunks = device_sm_count() * 2;
   p.L = lcdf_layout(max_segments);
   p.fallback_sort = sort_plan(n, 30);
   p.fallback_unique = unique_plan(n);
@@ -833,17 +866,23 @@ LsortPlan lsort_plan(int n, int nb, int max_segments) {
   // part (its bases and per-tile histograms follow, written before use)
   p.stats_off = take(sizeof(LsortStats));
   p.counter_off = take(64);
+  p.cursor_off = take(4 * (size_t)nb);
   p.lookback_off = 0;  // unused: buckets publish counts, a scan packs them
   p.uniq_ctrl_off = take(p.fallback_unique.bytes);
   p.sort_ctrl_off = take(p.fallback_sort.bytes);
   p.zero_bytes = p.sort_ctrl_off + p.fallback_sort.zero_bytes;
   // not zeroed:
-  p.hist_off = take(4 * (size_t)p.chunks * nb);
-  p.totals_off = take(4 * (size_t)nb);
   p.starts_off = take(4 * (size_t)(nb + 1));
   p.ucount_off = take(4 * (size_t)nb);
   p.uoff_off = take(4 * (size_t)nb);
-  p.bkeys_off = take(4 * (size_t)(n > 0 ? n : 1));
+  p.counts_off = take(4 * (size_t)nb);
+  // bucket capacity of the one-pass bin (a bucket past it sends the sort to
+  // the fallback): what the bucket kernel's sorted forms take (kCap keys;
+  // only a bitmap takes more), or 2x the mean bucket when that is larger; a
+  // whole number of 128-byte lines
+  const size_t mean = ((size_t)(n > 0 ? n : 1) + nb - 1) / nb;
+  p.cap = (uint32_t)align_up(std::max<size_t>((size_t)kCap, 2 * mean), 32);
+  p.bkeys_off = take(4 * (size_t)nb * p.cap);
   p.alt_off = take(4 * (size_t)(n > 0 ? n : 1));
   p.bytes = o;
   return p;
@@ -857,23 +896,20 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   LsortStats* stats = reinterpret_cast<LsortStats*>(ws + p.stats_off);
   uint32_t* counter = reinterpret_cast<uint32_t*>(ws + p.counter_off);
   uint32_t* gate = counter + 1;
-  uint32_t* hist = reinterpret_cast<uint32_t*>(ws + p.hist_off);
-  uint32_t* totals = reinterpret_cast<uint32_t*>(ws + p.totals_off);
   uint32_t* starts = reinterpret_cast<uint32_t*>(ws + p.starts_off);
   uint32_t* ucount = reinterpret_cast<uint32_t*>(ws + p.ucount_off);
   uint32_t* uoff = reinterpret_cast<uint32_t*>(ws + p.uoff_off);
   uint32_t* bkeys = reinterpret_cast<uint32_t*>(ws + p.bkeys_off);
   uint32_t* alt = reinterpret_cast<uint32_t*>(ws + p.alt_off);
-  const size_t hsm = lsort_hist_smem(p.nb, p.L.max_knots);
-  if (hsm > (size_t)kLsortMaxSmem) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(lsort_hist_kernel<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(ws + p.cursor_off);
+  uint32_t* counts = reinterpret_cast<uint32_t*>(ws + p.counts_off);
+  const size_t bsm = lsort_bin_smem(p.nb);
+  if (bsm > (size_t)kLsortMaxSmem) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(lsort_bin_kernel<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(lsort_hist_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hsm);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(lsort_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hsm);
+    e = cudaFuncSetAttribute(lsort_bin_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bsm);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(lsort_bucket_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BucketSmem));
@@ -881,20 +917,28 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   e = cudaMemsetAsync(ws, 0, p.zero_bytes, s);
   if (e != cudaSuccess) return e;
   mark(rec, s);
+  // one 1,024-thread CTA per SM; tiles of 1,024 x items keys, items as large
+  // as keeps every SM busy (kBinItems for large clouds, 1 for frame-sized ones)
+  const int sms = device_sm_count();
+  const int items =
+      std::max(1, std::min(kBinItems, (int)(((long long)n + (long long)sms * kBinThreads - 1) /
+                                            ((long long)sms * kBinThreads))));
+  const int tiles = (n + kBinThreads * items - 1) / (kBinThreads * items);
+  const int grid = std::min(sms, tiles);
   if (pts)
-    lsort_hist_kernel<true><<<p.chunks, kLsThreads, hsm, s>>>(pts, keys, n, min_coord, range,
-                                                              blob, p.L, hist, p.nb, status);
+    lsort_bin_kernel<true><<<grid, kBinThreads, bsm, s>>>(pts, keys, n, min_coord, range, blob, p.L,
+                                                          p.nb, p.cap, items, cursor, bkeys,
+                                                          status);
   else
-    lsort_hist_kernel<false><<<p.chunks, kLsThreads, hsm, s>>>(nullptr, keys, n, 0.f, 1.f, blob,
-                                                               p.L, hist, p.nb, status);
+    lsort_bin_kernel<false><<<grid, kBinThreads, bsm, s>>>(nullptr, keys, n, 0.f, 1.f, blob, p.L,
+                                                           p.nb, p.cap, items, cursor, bkeys,
+                                                           status);
   mark(rec, s);
-  lsort_offsets_kernel<<<(p.nb + 31) / 32, 256, 0, s>>>(hist, p.chunks, p.nb, totals);
-  lsort_scan_kernel<<<1, 1024, 0, s>>>(totals, p.nb, n, threshold, blob, starts, stats);
+  lsort_bin_stats_kernel<<<1, 1024, 0, s>>>(cursor, p.nb, n, p.cap, threshold, blob, starts, counts,
+                                            stats);
   mark(rec, s);
-  lsort_scatter_kernel<<<p.chunks, kLsThreads, hsm, s>>>(keys, n, blob, p.L, hist, starts, p.nb,
-                                                         bkeys, stats);
-  mark(rec, s);
-  lsort_bucket_kernel<<<p.nb, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, starts, ucount, stats);
+  lsort_bucket_kernel<<<p.nb, kBkThreads, sizeof(BucketSmem), s>>>(bkeys, starts, ucount, stats,
+                                                                   counts);
   mark(rec, s);
   lsort_uscan_kernel<<<1, 1024, 0, s>>>(ucount, p.nb, uoff, d_unique, stats);
   lsort_compact_kernel<<<p.nb, 256, 0, s>>>(bkeys, starts, ucount, uoff, out, stats);
@@ -941,7 +985,8 @@ LearnedBuildLayout learned_layout(int n, int cap, int nb, int max_segments) {
 bool lsort_args_ok(int n, int nb, int max_segments) {
   return n >= 0 && n <= OCT_MAX_N && nb >= 1 && nb <= 65536 && max_segments >= 1 &&
          max_segments <= octgb::kLcdfMaxSegments &&
-         octgb::lsort_hist_smem(nb, max_segments) <= (size_t)octgb::kLsortMaxSmem;
+         octgb::lsort_hist_smem(nb, max_segments) <= (size_t)octgb::kLsortMaxSmem &&
+         octgb::lsort_bin_smem(nb) <= (size_t)octgb::kLsortMaxSmem;
 }
 
 int fail_cuda(cudaError_t e, const char* where) {

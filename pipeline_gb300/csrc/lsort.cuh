@@ -13,7 +13,7 @@ struct LsortStats {
   uint32_t max_bucket;      // largest bucket
   uint32_t n;
   float overflow_frac;      // overflow_keys / n
-  uint32_t skip;            // set before the scatter when overflow_frac > threshold
+  uint32_t skip;            // set after the bin pass: the bucket stage does not run
   uint32_t bitmap_buckets;  // buckets sorted through a shared-memory bitmap
   uint32_t radix_buckets;   // ... through the shared-memory radix sort
   uint32_t bitonic_buckets; // ... through the bitonic sort
@@ -22,12 +22,13 @@ struct LsortStats {
 static_assert(sizeof(LsortStats) == 48, "LsortStats is 12 words");
 
 struct LsortPlan {
-  int n, nb, chunks;
+  int n, nb;
   LcdfLayout L;
   SortPlan fallback_sort;
   ScanPlan fallback_unique;
   size_t stats_off, counter_off, lookback_off, sort_ctrl_off, uniq_ctrl_off, zero_bytes;
-  size_t hist_off, totals_off, starts_off, ucount_off, uoff_off, bkeys_off, alt_off, bytes;
+  size_t cursor_off, starts_off, counts_off, ucount_off, uoff_off, bkeys_off, alt_off, bytes;
+  uint32_t cap;  // keys per bucket range of bkeys
 };
 
 LsortPlan lsort_plan(int n, int nb, int max_segments);

@@ -66,6 +66,21 @@ def test_lsort_forced_fallback_is_exact():
     assert out.cpu().numpy().view(np.uint32).tobytes() == np.unique(keys).tobytes()
 
 
+def test_bucket_past_bin_capacity_falls_back_exact():
+    """A model applied to keys it was not fit on: bucket 0 receives far more
+    keys than a bucket range of the one-pass bin holds (16,384 here), so the
+    sort falls back to the LSD passes, and the result is still exact."""
+    from pipeline_gb300.pipeline import lsort_unique
+
+    rng = np.random.default_rng(17)
+    m = fitted(rng.integers(0, 1 << 30, 1 << 20).astype(np.uint32), n_buckets=1024)
+    keys = rng.integers(0, 1 << 19, 300_000).astype(np.uint32)  # all in bucket 0
+    out, stats = lsort_unique(dev_keys(keys), m)
+    assert stats["fallback"] == 1 and stats["skip"] == 1, stats
+    assert stats["max_bucket"] > 16384, stats
+    assert out.cpu().numpy().view(np.uint32).tobytes() == np.unique(keys).tobytes()
+
+
 def test_trained_model_balances_buckets_where_key_bits_do_not():
     """What the trained CDF gains over bucketing by key bits on clustered keys:
     the largest bucket and the share of keys in oversized buckets."""
