@@ -56,6 +56,22 @@ def test_lsort_unique_exact(kind, n):
     assert stats["fallback"] == 0, stats
 
 
+@pytest.mark.parametrize("n", [1023, 1025, 155_649, 466_945, 1_089_537, 1_245_185, 2_000_001])
+def test_lsort_unique_tile_shapes(n):
+    """The one-pass bin sizes its tiles to the input (1,024 to 8,192 keys so
+    that every SM gets tiles): sizes around those steps, with partial last
+    tiles and runs of equal keys (which the bin leaves out of the buckets)."""
+    from pipeline_gb300.pipeline import lsort_unique
+
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 1 << 30, n).astype(np.uint32)
+    keys[5::9] = keys[4::9][: len(keys[5::9])]  # equal neighbours
+    m = fitted(keys, n_buckets=1024)
+    out, stats = lsort_unique(dev_keys(keys), m)
+    assert out.cpu().numpy().view(np.uint32).tobytes() == np.unique(keys).tobytes()
+    assert stats["fallback"] == 0, stats
+
+
 def test_lsort_forced_fallback_is_exact():
     from pipeline_gb300.pipeline import lsort_unique
 
