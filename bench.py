@@ -608,13 +608,22 @@ def clustered_workload(dev, flush, reps):
         plain.codes[: pc.n_unique], learned.codes[: lc.n_unique])
     t_plain = _time_events(lambda: plain.build(pts, MIN_COORD, RANGE), reps, stream, flush)
     t_learned = _time_events(lambda: learned.build(pts, MIN_COORD, RANGE), reps, stream, flush)
+    # the same builds replayed from CUDA graphs (as the headline step is)
+    plain_g = _graph_of(lambda: plain.build(pts, MIN_COORD, RANGE), dev)
+    learned_g = _graph_of(lambda: learned.build(pts, MIN_COORD, RANGE), dev)
+    t_plain_g = _time_events(plain_g, reps, stream, flush) if plain_g else None
+    t_learned_g = _time_events(learned_g, reps, stream, flush) if learned_g else None
     st = learned.lsort_stats()
     h = model.header()
     return {"workload": "clustered_16m: 64 anisotropic Gaussians (sigma 0.5-20% of the box) + 5% "
                         "uniform noise, 16,777,216 points, seed 7",
             "n_unique": pc.n_unique, "plain_mpts": round(n / t_plain / 1e3, 1),
             "learned_mpts": round(n / t_learned / 1e3, 1),
-            "speedup": round(t_plain / t_learned, 3), "bit_exact": bool(exact),
+            "speedup": round(t_plain / t_learned, 3),
+            "plain_graph_mpts": round(n / t_plain_g / 1e3, 1) if t_plain_g else None,
+            "learned_graph_mpts": round(n / t_learned_g / 1e3, 1) if t_learned_g else None,
+            "speedup_graph": round(t_plain_g / t_learned_g, 3) if t_plain_g and t_learned_g else None,
+            "bit_exact": bool(exact),
             "overflow_frac": round(st["overflow_frac"], 5), "fallback": st["fallback"],
             "max_bucket": st["max_bucket"], "fit_loss": h["loss"], "fit_ms": round(fit_ms, 2),
             "fit": "4096 segments, 262,144 sampled Morton codes, 100 Adam steps"}
