@@ -662,7 +662,11 @@ __device__ __forceinline__ bool lb_first_of_its_key(uint32_t k) {
 }
 
 // CTAs walk the tiles from a capped grid, so each stages the model's lookup
-// tables once for several tiles.
+// tables once for several tiles. A warp takes kLbRows rows of 32 consecutive
+// keys at a time (their loads in flight together); rows start at the tile's
+// first key + 32 r in both kernels, so both drop the same repeats.
+constexpr int kLbRows = 4;
+
 __global__ void __launch_bounds__(256)
     lb_hist_kernel(const uint32_t* __restrict__ keys, const int4* __restrict__ tiles, int n_tiles,
                    const char* __restrict__ blob, LcdfLayout L, int nb,
@@ -676,10 +680,17 @@ __global__ void __launch_bounds__(256)
     for (int b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0;
     __syncthreads();
     const int4 d = tiles[t];
-    for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
-      const int i = base + lane;
-      const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;  // no code reaches 2^32 - 1
-      if (lb_first_of_its_key(k)) atomicAdd(&s_hist[bucket_of(q, k)], 1u);
+    for (int base = d.x + (int)(threadIdx.x >> 5) * 32 * kLbRows; base < d.y;
+         base += blockDim.x * kLbRows) {
+      uint32_t k[kLbRows];
+#pragma unroll
+      for (int u = 0; u < kLbRows; ++u) {
+        const int i = base + u * 32 + lane;
+        k[u] = i < d.y ? keys[i] : 0xffffffffu;  // no code reaches 2^32 - 1
+      }
+#pragma unroll
+      for (int u = 0; u < kLbRows; ++u)
+        if (lb_first_of_its_key(k[u])) atomicAdd(&s_hist[bucket_of(q, k[u])], 1u);
     }
     __syncthreads();
     uint32_t* row = tile_off + (size_t)t * nb;
@@ -745,10 +756,17 @@ __global__ void __launch_bounds__(256)
     for (int b = threadIdx.x; b < nb; b += blockDim.x) cursor[b] = row[b];
     __syncthreads();
     const int4 d = tiles[t];
-    for (int base = d.x + (int)(threadIdx.x & ~31u); base < d.y; base += blockDim.x) {
-      const int i = base + lane;
-      const uint32_t k = i < d.y ? keys[i] : 0xffffffffu;
-      if (lb_first_of_its_key(k)) out[atomicAdd(&cursor[bucket_of(q, k)], 1u)] = k;
+    for (int base = d.x + (int)(threadIdx.x >> 5) * 32 * kLbRows; base < d.y;
+         base += blockDim.x * kLbRows) {
+      uint32_t k[kLbRows];
+#pragma unroll
+      for (int u = 0; u < kLbRows; ++u) {
+        const int i = base + u * 32 + lane;
+        k[u] = i < d.y ? keys[i] : 0xffffffffu;
+      }
+#pragma unroll
+      for (int u = 0; u < kLbRows; ++u)
+        if (lb_first_of_its_key(k[u])) out[atomicAdd(&cursor[bucket_of(q, k[u])], 1u)] = k[u];
     }
     __syncthreads();
   }
