@@ -439,13 +439,25 @@ __global__ void __launch_bounds__(kBkThreads, 3)
   const uint32_t lo = starts[b];
   const int cnt = (int)(counts ? counts[b] : starts[b + 1] - lo);
   const bool cached = cnt <= kBkCache;
-  // keys -> cache, and the key span of the bucket
+  // keys -> cache, and the key span of the bucket (four loads per thread in
+  // flight)
   uint32_t kmin = 0xffffffffu, kmax = 0;
-  for (int i = tid; i < cnt; i += kBkThreads) {
-    const uint32_t k = bkeys[lo + i];
-    if (cached) S.buf[i] = k;
-    kmin = min(kmin, k);
-    kmax = max(kmax, k);
+  for (int i0 = tid; i0 < cnt; i0 += 4 * kBkThreads) {
+    uint32_t k[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * kBkThreads;
+      k[u] = i < cnt ? bkeys[lo + i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * kBkThreads;
+      if (i < cnt) {
+        if (cached) S.buf[i] = k[u];
+        kmin = min(kmin, k[u]);
+        kmax = max(kmax, k[u]);
+      }
+    }
   }
   kmin = __reduce_min_sync(0xffffffffu, kmin);
   kmax = __reduce_max_sync(0xffffffffu, kmax);
@@ -521,9 +533,20 @@ __global__ void __launch_bounds__(kBkThreads, 3)
         atomicOr(&bm[r >> 5], 1u << (r & 31));
       }
     } else {
-      for (int i = tid; i < cnt; i += kBkThreads) {
-        const uint32_t r = bkeys[lo + i] - kmin;
-        atomicOr(&bm[r >> 5], 1u << (r & 31));
+      for (int i0 = tid; i0 < cnt; i0 += 4 * kBkThreads) {
+        uint32_t k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * kBkThreads;
+          k[u] = i < cnt ? bkeys[lo + i] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (i0 + u * kBkThreads < cnt) {
+            const uint32_t r = k[u] - kmin;
+            atomicOr(&bm[r >> 5], 1u << (r & 31));
+          }
+        }
       }
     }
     __syncthreads();
@@ -617,6 +640,26 @@ __global__ void __launch_bounds__(1024)
   if (threadIdx.x == 0) *d_unique = (int)total;
 }
 
+// dst[0, n) = src[0, n) by the whole block, four loads per thread in flight.
+__device__ __forceinline__ void copy_run(uint32_t* __restrict__ dst,
+                                         const uint32_t* __restrict__ src, uint32_t n) {
+  constexpr int U = 4;
+  const uint32_t step = blockDim.x * U;
+  for (uint32_t i0 = threadIdx.x; i0 < n; i0 += step) {
+    uint32_t v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t i = i0 + (uint32_t)u * blockDim.x;
+      if (i < n) v[u] = src[i];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t i = i0 + (uint32_t)u * blockDim.x;
+      if (i < n) dst[i] = v[u];
+    }
+  }
+}
+
 // One block per bucket: its unique run, from the front of its bkeys range to
 // its place in the output.
 __global__ void __launch_bounds__(256)
@@ -625,10 +668,7 @@ __global__ void __launch_bounds__(256)
                          uint32_t* __restrict__ out, const LsortStats* __restrict__ stats) {
   if (stats->fallback) return;
   const int b = blockIdx.x;
-  const uint32_t* src = bkeys + starts[b];
-  uint32_t* dst = out + uoff[b];
-  const int c = (int)ucount[b];
-  for (int i = threadIdx.x; i < c; i += 256) dst[i] = src[i];
+  copy_run(out + uoff[b], bkeys + starts[b], ucount[b]);
 }
 
 // ----------------------------------------------------- batched learned sort --
@@ -800,10 +840,7 @@ __global__ void __launch_bounds__(256)
                       uint32_t* __restrict__ out, const LsortStats* __restrict__ stats) {
   if (stats->fallback) return;
   const int g = blockIdx.x;
-  const uint32_t n = ucount[g];
-  const uint32_t* src = bkeys + bstart[g];
-  uint32_t* dst = out + uoff[g];
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  copy_run(out + uoff[g], bkeys + bstart[g], ucount[g]);
 }
 
 __global__ void __launch_bounds__(256)
