@@ -80,6 +80,21 @@ def algorithmic_bytes(n, u, b, m, msd=False):
     }
 
 
+def cloud_bytes(counts) -> int:
+    """Algorithmic bytes of building clouds whose counts are (n, U, U-1, M)
+    rows: the LSD-form accounting of algorithmic_bytes, summed over clouds
+    (every form of stages 2-3 produces the same outputs)."""
+    return int(sum(sum(algorithmic_bytes(int(n), int(u), int(b), int(m)).values())
+                   for n, u, b, m in counts))
+
+
+def hbm_frac(nbytes: int, ms: float | None):
+    """nbytes moved in ms, as a fraction of the measured HBM copy peak."""
+    if not ms:
+        return None
+    return round(nbytes / (ms * 1e-3) / (peaks()[0] * 1e9), 4)
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -615,6 +630,7 @@ def clustered_workload(dev, flush, reps):
     t_learned_g = _time_events(learned_g, reps, stream, flush) if learned_g else None
     st = learned.lsort_stats()
     h = model.header()
+    alg = cloud_bytes([(n, pc.n_unique, pc.n_brt, pc.n_oct)])
     return {"workload": "clustered_16m: 64 anisotropic Gaussians (sigma 0.5-20% of the box) + 5% "
                         "uniform noise, 16,777,216 points, seed 7",
             "n_unique": pc.n_unique, "plain_mpts": round(n / t_plain / 1e3, 1),
@@ -623,6 +639,9 @@ def clustered_workload(dev, flush, reps):
             "plain_graph_mpts": round(n / t_plain_g / 1e3, 1) if t_plain_g else None,
             "learned_graph_mpts": round(n / t_learned_g / 1e3, 1) if t_learned_g else None,
             "speedup_graph": round(t_plain_g / t_learned_g, 3) if t_plain_g and t_learned_g else None,
+            "hbm_frac_lsd_bytes": {"plain": hbm_frac(alg, t_plain), "learned": hbm_frac(alg, t_learned),
+                                   "plain_graph": hbm_frac(alg, t_plain_g),
+                                   "learned_graph": hbm_frac(alg, t_learned_g)},
             "bit_exact": bool(exact),
             "overflow_frac": round(st["overflow_frac"], 5), "fallback": st["fallback"],
             "max_bucket": st["max_bucket"], "fit_loss": h["loss"], "fit_ms": round(fit_ms, 2),
@@ -677,6 +696,7 @@ def batched_workload(dev, flush, reps):
         g = b.cloud_result(c, counts)
         exact &= r["oct_nodes"].tobytes() == g["oct_nodes"].tobytes()
     t_batch = _time_events(b.replay, reps, stream, flush)
+    alg = cloud_bytes([(sz, u, bb, m) for sz, (u, bb, m, _) in zip(sizes, counts)])
     # the same build with its octree-stage kernels fed by a work queue of
     # persistent CTAs instead of one CTA per tile
     from pipeline_gb300 import _lib
@@ -694,6 +714,7 @@ def batched_workload(dev, flush, reps):
     return {"workload": "batched_512: 512 clouds, sizes log-uniform in [1K, 1M] (seed 11), even "
                         "uniform, odd 8-Gaussian mixtures; one CUDA-graph-captured batched build",
             "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
+            "batched_hbm_frac_lsd_bytes": hbm_frac(alg, t_batch),
             "batched_work_queue_mpts": round(total / t_queue / 1e3, 1),
             "per_cloud_loop_mpts": round(total / t_loop / 1e3, 1),
             "speedup": round(t_loop / t_batch, 3),
@@ -783,6 +804,7 @@ def frames_workload(dev, flush, reps):
     lb_exact = lbb.same_results(b)
     t_batch = _time_events(b.replay, reps, stream, flush)
     t_lbatch = _time_events(lbb.replay, reps, stream, flush)
+    alg = cloud_bytes([(sz, u, bb, m) for sz, (u, bb, m, _) in zip(sizes, counts)])
     t_plain = _time_events(plain_loop, max(2, reps // 4), stream, flush)
     t_learn = _time_events(learned_loop, max(2, reps // 4), stream, flush)
     plain_graph = _graph_of(plain_loop, dev)
@@ -800,6 +822,8 @@ def frames_workload(dev, flush, reps):
             "per_frame_learned_graph_mpts": round(total / t_learn_g / 1e3, 1) if t_learn_g else None,
             "batched_vs_graph_loop": round(t_plain_g / t_batch, 3) if t_plain_g else None,
             "learned_batched_mpts": round(total / t_lbatch / 1e3, 1),
+            "hbm_frac_lsd_bytes": {"batched": hbm_frac(alg, t_batch),
+                                   "learned_batched": hbm_frac(alg, t_lbatch)},
             "learned_batched_vs_batched": round(t_batch / t_lbatch, 3),
             "learned_batched_vs_graph_loop": round(t_plain_g / t_lbatch, 3) if t_plain_g else None,
             "learned_batched_vs_stream_loop": round(t_plain / t_lbatch, 3),

@@ -898,11 +898,6 @@ cudaError_t launch_lbatch_sort(const LbatchArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// Gate for the fallback launches: 1 when the learned path gave up.
-__global__ void lsort_gate_kernel(const LsortStats* stats, uint32_t* gate) {
-  *gate = stats->fallback ? 1u : 0u;
-}
-
 // ------------------------------------------------------------------ plan --
 LsortPlan lsort_plan(int n, int nb, int max_segments) {
   LsortPlan p{};
@@ -920,9 +915,7 @@ LsortPlan lsort_plan(int n, int nb, int max_segments) {
   // zeroed each run: everything up to the end of the fallback sort's zeroed
   // part (its bases and per-tile histograms follow, written before use)
   p.stats_off = take(sizeof(LsortStats));
-  p.counter_off = take(64);
   p.cursor_off = take(4 * (size_t)nb);
-  p.lookback_off = 0;  // unused: buckets publish counts, a scan packs them
   p.uniq_ctrl_off = take(p.fallback_unique.bytes);
   p.sort_ctrl_off = take(p.fallback_sort.bytes);
   p.zero_bytes = p.sort_ctrl_off + p.fallback_sort.zero_bytes;
@@ -949,8 +942,9 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
                          Recorder* rec) {
   if (n <= 0) return cudaMemsetAsync(d_unique, 0, sizeof(int), s);
   LsortStats* stats = reinterpret_cast<LsortStats*>(ws + p.stats_off);
-  uint32_t* counter = reinterpret_cast<uint32_t*>(ws + p.counter_off);
-  uint32_t* gate = counter + 1;
+  // the fallback launches run only when the learned path gave up: their gate
+  // is the fallback flag itself (final once the bucket kernel is done)
+  uint32_t* gate = &stats->fallback;
   uint32_t* starts = reinterpret_cast<uint32_t*>(ws + p.starts_off);
   uint32_t* ucount = reinterpret_cast<uint32_t*>(ws + p.ucount_off);
   uint32_t* uoff = reinterpret_cast<uint32_t*>(ws + p.uoff_off);
@@ -1001,7 +995,6 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // Fallback: OneSweep + unique on the original keys, gated on the flag.
-  lsort_gate_kernel<<<1, 1, 0, s>>>(stats, gate);
   char* sc = ws + p.sort_ctrl_off;
   e = launch_histogram_gated(keys, &p.fallback_sort, sc, gate, s);
   if (e != cudaSuccess) return e;

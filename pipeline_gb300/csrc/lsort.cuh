@@ -26,7 +26,7 @@ struct LsortPlan {
   LcdfLayout L;
   SortPlan fallback_sort;
   ScanPlan fallback_unique;
-  size_t stats_off, counter_off, lookback_off, sort_ctrl_off, uniq_ctrl_off, zero_bytes;
+  size_t stats_off, sort_ctrl_off, uniq_ctrl_off, zero_bytes;
   size_t cursor_off, starts_off, counts_off, ucount_off, uoff_off, bkeys_off, alt_off, bytes;
   uint32_t cap;  // keys per bucket range of bkeys
 };
