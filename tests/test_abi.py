@@ -54,6 +54,20 @@ def test_workspace_sizes_are_host_computable():
     assert lib.oct_sort_workspace_bytes(n, 30) < 4 * n
 
 
+@pytest.mark.parametrize("n,nb", [(1000, 4096), (1 << 20, 1024), (1 << 24, 4096), (1 << 24, 256)])
+def test_learned_workspace_holds_every_bucket_range(n, nb):
+    """The learned sort bins keys into one fixed range per bucket: at least
+    4 B x nb x max(16,384, 2 n / nb) keys (rounded to whole 128-byte lines)."""
+    lib = _lib.load()
+    mean = -(-n // nb)
+    cap = -(-max(16384, 2 * mean) // 32) * 32
+    ws = lib.oct_lsort_workspace_bytes(n, nb, 4096)
+    assert ws >= 4 * nb * cap
+    assert ws < 4 * nb * cap + 16 * n + (64 << 20)  # the rest: keys, fallback sort, tables
+    assert lib.oct_build_learned_workspace_bytes(n, n, nb, 4096) > ws
+    assert lib.oct_lsort_workspace_bytes(n, 1 << 20, 4096) == 0  # bucket tables past shared memory
+
+
 def test_invalid_arguments_rejected_before_any_device_work():
     lib = _lib.load()
     assert lib.oct_morton_encode(None, None, -1, 0.0, 1.0, None, None) == _lib.OCT_ERR_INVALID_ARG
