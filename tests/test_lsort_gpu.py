@@ -140,6 +140,29 @@ def test_learned_build_matches_oracle(kind):
     assert b.lsort_stats()["fallback"] == 0
 
 
+def test_learned_build_with_a_foreign_model_falls_back_exact():
+    """A learned build from points whose codes all fall in one bucket of the
+    model (fit on uniform codes): the one-pass bin overflows that bucket's
+    range, the build takes the fallback sort and still equals the oracle."""
+    from pipeline_gb300.pipeline import LearnedOctreeBuilder
+
+    rng = np.random.default_rng(23)
+    m = fitted(rng.integers(0, 1 << 30, 1 << 20).astype(np.uint32), n_buckets=1024)
+    n = 300_000
+    pts = np.zeros((n, 4), np.float32)
+    pts[:, :3] = rng.uniform(0.0, 60.0, (n, 3))  # codes below 2^18: bucket 0
+    pts[:, 3] = 1.0
+    b = LearnedOctreeBuilder(n, m)
+    b.build(torch.from_numpy(pts).cuda(), 0.0, 1024.0)
+    res = b.result()
+    st = b.lsort_stats()
+    assert st["fallback"] == 1 and st["max_bucket"] > 16384, st
+    want = O.build_all(pts, 0.0, 1024.0, threads=4)
+    assert (res["n_unique"], res["n_oct"], res["status"]) == (want["n_unique"], want["n_oct"], 0)
+    for key in ["sorted_unique", "left_child", "parent", "prefix_sum", "oct_nodes"]:
+        assert res[key].tobytes() == np.asarray(want[key]).tobytes(), key
+
+
 @pytest.mark.parametrize("form", ["bitmap", "radix", "bitonic", "wide_bitmap"])
 def test_each_bucket_form_exact(form):
     """Inputs chosen so the buckets take one shared-memory form: dense keys
