@@ -811,6 +811,8 @@ def frames_workload(dev, flush, reps):
     learned_graph = _graph_of(learned_loop, dev)
     t_plain_g = _time_events(plain_graph, max(2, reps // 4), stream, flush) if plain_graph else None
     t_learn_g = _time_events(learned_graph, max(2, reps // 4), stream, flush) if learned_graph else None
+    e2e = frames_e2e(b, lbb, single, learned, pts, test_f, sizes, mins, ranges, stream, flush,
+                     max(2, reps // 4))
     return {"workload": "frames: 224 scan-like frames (32-255) of 122,880 points, per-frame "
                         "min/range; model fit on frames 0-31 (1024 segments, 512 buckets)",
             "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
@@ -832,7 +834,73 @@ def frames_workload(dev, flush, reps):
             "learned_batched_max_bucket": lb_stats["max_bucket"],
             "learned_batched_fit_ms": round(fit_lb_ms, 2),
             "bit_exact_spot_check": bool(exact), "learned_fallbacks_in_spot_check": int(fallbacks),
-            "overflow_frac_max": round(max(overflow), 5), "fit_loss": model.header()["loss"]}
+            "overflow_frac_max": round(max(overflow), 5), "fit_loss": model.header()["loss"],
+            "e2e": e2e}
+
+
+def frames_e2e(b, lbb, single, learned, pts, test_f, sizes, mins, ranges, stream, flush, reps):
+    """The frames end to end: every frame's points copied in from pinned host
+    memory and its OctNodes copied back (sizes from the counts read back
+    first), either all frames in one batched build (plain or learned) or
+    frame by frame through the single-cloud builders, as a per-cloud pipeline
+    does. Mpoints/s over the same points and bytes."""
+    import torch
+
+    total = int(sum(sizes))
+    pin_pts = torch.from_numpy(np.concatenate(test_f, 0)).pin_memory()
+    host_nodes = torch.empty(tuple(b.nodes.shape), dtype=b.nodes.dtype).pin_memory()
+    host_counts = torch.empty(tuple(b.counts.shape), dtype=b.counts.dtype).pin_memory()
+    host_one = torch.empty(4, dtype=torch.int32).pin_memory()
+    ns = [int(x) for x in b.node_start]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    pin_views = [pin_pts[offs[c]:offs[c + 1]] for c in range(len(sizes))]
+    dev_buf = torch.empty((max(sizes), 4), dtype=torch.float32, device=pts.device)
+    moved = {"h2d": 0, "d2h": 0}
+
+    def batched(builder):
+        def step():
+            pts.copy_(pin_pts, non_blocking=True)
+            builder.replay()
+            host_counts.copy_(builder.counts, non_blocking=True)
+            stream.synchronize()  # the OctNode counts size the copies
+            cnt = host_counts.numpy().reshape(-1, 4)
+            d2h = 0
+            for c in range(len(sizes)):
+                m = int(cnt[c, 2])
+                if m:
+                    host_nodes[ns[c]:ns[c] + m].copy_(builder.nodes[ns[c]:ns[c] + m],
+                                                      non_blocking=True)
+                    d2h += m * 60
+            moved.update(h2d=pin_pts.numel() * 4, d2h=d2h + host_counts.numel() * 4)
+        return step
+
+    def per_frame(builder):
+        def step():
+            for c in range(len(sizes)):
+                n = int(sizes[c])
+                dev_buf[:n].copy_(pin_views[c], non_blocking=True)
+                builder.build(dev_buf[:n], mins[32 + c], ranges[32 + c])
+                host_one.copy_(builder.d_counts, non_blocking=True)
+                stream.synchronize()
+                m = int(host_one[2])
+                if m:
+                    host_nodes[ns[c]:ns[c] + m].copy_(builder.nodes[:m], non_blocking=True)
+        return step
+
+    t = {}
+    for name, fn in (("batched", batched(b)), ("learned_batched", batched(lbb)),
+                     ("per_frame_plain", per_frame(single)),
+                     ("per_frame_learned", per_frame(learned))):
+        fn()
+        torch.cuda.synchronize()
+        t[name] = _time_events(fn, reps, stream, flush)
+    mp = {k: round(total / v / 1e3, 1) for k, v in t.items()}
+    return {"mode": "host points in, OctNodes out, each frame's node count read back first",
+            "h2d_bytes": moved["h2d"], "d2h_bytes": moved["d2h"],
+            **{f"{k}_mpts": v for k, v in mp.items()},
+            "learned_batched_vs_per_frame_plain": round(t["per_frame_plain"] / t["learned_batched"], 3),
+            "batched_vs_per_frame_plain": round(t["per_frame_plain"] / t["batched"], 3),
+            "learned_batched_vs_batched": round(t["batched"] / t["learned_batched"], 3)}
 
 
 def sort_bar_workload(dev, flush, reps, pts):
