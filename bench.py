@@ -708,6 +708,9 @@ def batched_workload(dev, flush, reps):
     t_queue = _time_events(b_queue.replay, reps, stream, flush)
     del b_queue
     t_loop = _time_events(loop, max(2, reps // 4), stream, flush)
+    e2e = batches_e2e({"batched": b}, {"per_cloud_plain": single}, pts, np.concatenate(clouds, 0),
+                      sizes, [MIN_COORD] * len(sizes), [RANGE] * len(sizes), stream, flush,
+                      max(2, reps // 4))
     loop_graph = _graph_of(loop, dev)
     t_loop_graph = _time_events(loop_graph, max(2, reps // 4), stream, flush) if loop_graph else None
     autotune.set_config(old_cfg)
@@ -721,6 +724,7 @@ def batched_workload(dev, flush, reps):
             "per_cloud_loop_graph_mpts": round(total / t_loop_graph / 1e3, 1) if t_loop_graph else None,
             "speedup_vs_graph_loop": round(t_loop_graph / t_batch, 3) if t_loop_graph else None,
             "bit_exact_spot_check": bool(exact),
+            "e2e": e2e,
             "autotuned_sort_shape": {"radix_bits": tuned["config"][0], "warps": tuned["config"][1],
                                      "items": tuned["config"][2], "candidates_ms": tuned["all"]}}
 
@@ -811,8 +815,11 @@ def frames_workload(dev, flush, reps):
     learned_graph = _graph_of(learned_loop, dev)
     t_plain_g = _time_events(plain_graph, max(2, reps // 4), stream, flush) if plain_graph else None
     t_learn_g = _time_events(learned_graph, max(2, reps // 4), stream, flush) if learned_graph else None
-    e2e = frames_e2e(b, lbb, single, learned, pts, test_f, sizes, mins, ranges, stream, flush,
-                     max(2, reps // 4))
+    e2e = batches_e2e({"batched": b, "learned_batched": lbb},
+                      {"per_frame_plain": single, "per_frame_learned": learned}, pts,
+                      np.concatenate(test_f, 0), sizes, mins[32:], ranges[32:], stream, flush,
+                      max(2, reps // 4))
+    e2e["learned_batched_vs_batched"] = round(e2e["learned_batched_mpts"] / e2e["batched_mpts"], 3)
     return {"workload": "frames: 224 scan-like frames (32-255) of 122,880 points, per-frame "
                         "min/range; model fit on frames 0-31 (1024 segments, 512 buckets)",
             "total_points": total, "batched_mpts": round(total / t_batch / 1e3, 1),
@@ -838,26 +845,29 @@ def frames_workload(dev, flush, reps):
             "e2e": e2e}
 
 
-def frames_e2e(b, lbb, single, learned, pts, test_f, sizes, mins, ranges, stream, flush, reps):
-    """The frames end to end: every frame's points copied in from pinned host
-    memory and its OctNodes copied back (sizes from the counts read back
-    first), either all frames in one batched build (plain or learned) or
-    frame by frame through the single-cloud builders, as a per-cloud pipeline
-    does. Mpoints/s over the same points and bytes."""
+def batches_e2e(batched: dict, single: dict, pts, host_pts, sizes, mins, ranges, stream, flush,
+                reps):
+    """Batched builds end to end: every cloud's points copied in from pinned
+    host memory and its OctNodes copied back (sizes from the node counts read
+    back first), either all clouds in one batched build (`batched`: name ->
+    captured batch builder) or cloud by cloud through a single-cloud builder
+    (`single`: name -> builder), as a per-cloud pipeline does. Mpoints/s over
+    the same points and bytes."""
     import torch
 
     total = int(sum(sizes))
-    pin_pts = torch.from_numpy(np.concatenate(test_f, 0)).pin_memory()
-    host_nodes = torch.empty(tuple(b.nodes.shape), dtype=b.nodes.dtype).pin_memory()
-    host_counts = torch.empty(tuple(b.counts.shape), dtype=b.counts.dtype).pin_memory()
+    any_b = next(iter(batched.values()))
+    pin_pts = torch.from_numpy(host_pts).pin_memory()
+    host_nodes = torch.empty(tuple(any_b.nodes.shape), dtype=any_b.nodes.dtype).pin_memory()
+    host_counts = torch.empty(tuple(any_b.counts.shape), dtype=any_b.counts.dtype).pin_memory()
     host_one = torch.empty(4, dtype=torch.int32).pin_memory()
-    ns = [int(x) for x in b.node_start]
+    ns = [int(x) for x in any_b.node_start]
     offs = np.concatenate([[0], np.cumsum(sizes)])
     pin_views = [pin_pts[offs[c]:offs[c + 1]] for c in range(len(sizes))]
     dev_buf = torch.empty((max(sizes), 4), dtype=torch.float32, device=pts.device)
     moved = {"h2d": 0, "d2h": 0}
 
-    def batched(builder):
+    def one_batch(builder):
         def step():
             pts.copy_(pin_pts, non_blocking=True)
             builder.replay()
@@ -874,12 +884,12 @@ def frames_e2e(b, lbb, single, learned, pts, test_f, sizes, mins, ranges, stream
             moved.update(h2d=pin_pts.numel() * 4, d2h=d2h + host_counts.numel() * 4)
         return step
 
-    def per_frame(builder):
+    def per_cloud(builder):
         def step():
             for c in range(len(sizes)):
                 n = int(sizes[c])
                 dev_buf[:n].copy_(pin_views[c], non_blocking=True)
-                builder.build(dev_buf[:n], mins[32 + c], ranges[32 + c])
+                builder.build(dev_buf[:n], float(mins[c]), float(ranges[c]))
                 host_one.copy_(builder.d_counts, non_blocking=True)
                 stream.synchronize()
                 m = int(host_one[2])
@@ -887,20 +897,20 @@ def frames_e2e(b, lbb, single, learned, pts, test_f, sizes, mins, ranges, stream
                     host_nodes[ns[c]:ns[c] + m].copy_(builder.nodes[:m], non_blocking=True)
         return step
 
+    runs = {**{k: one_batch(v) for k, v in batched.items()},
+            **{k: per_cloud(v) for k, v in single.items()}}
     t = {}
-    for name, fn in (("batched", batched(b)), ("learned_batched", batched(lbb)),
-                     ("per_frame_plain", per_frame(single)),
-                     ("per_frame_learned", per_frame(learned))):
+    for name, fn in runs.items():
         fn()
         torch.cuda.synchronize()
         t[name] = _time_events(fn, reps, stream, flush)
-    mp = {k: round(total / v / 1e3, 1) for k, v in t.items()}
-    return {"mode": "host points in, OctNodes out, each frame's node count read back first",
-            "h2d_bytes": moved["h2d"], "d2h_bytes": moved["d2h"],
-            **{f"{k}_mpts": v for k, v in mp.items()},
-            "learned_batched_vs_per_frame_plain": round(t["per_frame_plain"] / t["learned_batched"], 3),
-            "batched_vs_per_frame_plain": round(t["per_frame_plain"] / t["batched"], 3),
-            "learned_batched_vs_batched": round(t["batched"] / t["learned_batched"], 3)}
+    out = {"mode": "host points in, OctNodes out, each cloud's node count read back first",
+           "h2d_bytes": moved["h2d"], "d2h_bytes": moved["d2h"],
+           **{f"{k}_mpts": round(total / v / 1e3, 1) for k, v in t.items()}}
+    base = next(iter(single))
+    for k in batched:
+        out[f"{k}_vs_{base}"] = round(t[base] / t[k], 3)
+    return out
 
 
 def sort_bar_workload(dev, flush, reps, pts):
