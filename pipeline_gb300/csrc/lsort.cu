@@ -315,29 +315,50 @@ __device__ uint32_t* bucket_radix_sort(uint32_t* a, uint32_t* b, int cnt, uint32
     __syncthreads();
     uint32_t rk[kBkItems / 2];  // two 16-bit ranks per register; keys are re-read
     uint16_t* wh = S.whist[wid];
+    if (shift == 0) {
+      // The first pass needs no stability (the bucket's keys arrive in any
+      // order): a shared-memory atomic on the warp's 16-bit digit counter
+      // (the upper or lower half of its 32-bit word; a warp counts at most
+      // kBkItems * 32 keys, so no carry reaches the other half) ranks a key.
+      uint32_t* wh32 = reinterpret_cast<uint32_t*>(wh);
 #pragma unroll
-    for (int it = 0; it < kBkItems; ++it) {
-      if (it >= items) break;
-      const int idx = wid * seg + it * 32 + lane;
-      const bool valid = idx < cnt;
-      const uint32_t key = valid ? a[idx] : 0u;
-      const uint32_t dg = ((key - kmin) >> shift) & (kRsBins - 1);
-      uint32_t eq_lo = 0xffffffffu, eq_hi = 0xffffffffu;
-#pragma unroll
-      for (int bit = 0; bit < kHalf; ++bit) {
-        eq_lo &= ~(__ballot_sync(0xffffffffu, (dg >> bit) & 1u) ^ lane_bits[bit]);
-        eq_hi &= ~(__ballot_sync(0xffffffffu, (dg >> (kHalf + bit)) & 1u) ^ lane_bits[bit]);
+      for (int it = 0; it < kBkItems; ++it) {
+        if (it >= items) break;
+        const int idx = wid * seg + it * 32 + lane;
+        uint32_t r = 0;
+        if (idx < cnt) {
+          const uint32_t dg = (a[idx] - kmin) & (kRsBins - 1);
+          const uint32_t sh = 16u * (dg & 1u);
+          r = (atomicAdd(&wh32[dg >> 1], 1u << sh) >> sh) & 0xffffu;
+        }
+        if (it & 1) rk[it >> 1] |= r << 16;
+        else rk[it >> 1] = r;
       }
-      const uint32_t peers = __ballot_sync(0xffffffffu, valid) &
-                             __shfl_sync(0xffffffffu, eq_lo, (int)(dg & ((1u << kHalf) - 1u))) &
-                             __shfl_sync(0xffffffffu, eq_hi, (int)(dg >> kHalf));
-      const uint32_t before = valid ? wh[dg] : 0u;
-      const uint32_t r = before + __popc(peers & lt);
-      if (it & 1) rk[it >> 1] |= r << 16;
-      else rk[it >> 1] = r;
-      __syncwarp();
-      if (valid && (peers & lt) == 0) wh[dg] = (uint16_t)(before + __popc(peers));
-      __syncwarp();
+    } else {
+#pragma unroll
+      for (int it = 0; it < kBkItems; ++it) {
+        if (it >= items) break;
+        const int idx = wid * seg + it * 32 + lane;
+        const bool valid = idx < cnt;
+        const uint32_t key = valid ? a[idx] : 0u;
+        const uint32_t dg = ((key - kmin) >> shift) & (kRsBins - 1);
+        uint32_t eq_lo = 0xffffffffu, eq_hi = 0xffffffffu;
+#pragma unroll
+        for (int bit = 0; bit < kHalf; ++bit) {
+          eq_lo &= ~(__ballot_sync(0xffffffffu, (dg >> bit) & 1u) ^ lane_bits[bit]);
+          eq_hi &= ~(__ballot_sync(0xffffffffu, (dg >> (kHalf + bit)) & 1u) ^ lane_bits[bit]);
+        }
+        const uint32_t peers = __ballot_sync(0xffffffffu, valid) &
+                               __shfl_sync(0xffffffffu, eq_lo, (int)(dg & ((1u << kHalf) - 1u))) &
+                               __shfl_sync(0xffffffffu, eq_hi, (int)(dg >> kHalf));
+        const uint32_t before = valid ? wh[dg] : 0u;
+        const uint32_t r = before + __popc(peers & lt);
+        if (it & 1) rk[it >> 1] |= r << 16;
+        else rk[it >> 1] = r;
+        __syncwarp();
+        if (valid && (peers & lt) == 0) wh[dg] = (uint16_t)(before + __popc(peers));
+        __syncwarp();
+      }
     }
     __syncthreads();
     // per digit: exclusive offsets over warps, then digit starts over digits
