@@ -97,8 +97,8 @@ size_t lsort_hist_smem(int nb, int /*max_segments*/) {
 // One pass over the points (or keys) does what a histogram pass and a
 // scatter pass would: the Morton code, its bucket and its place in the
 // bucket. Bucket b owns the fixed range [b * cap, (b + 1) * cap) of bkeys.
-// CTAs (one per SM) walk tiles of up to kBinTile keys (1,024 x items, items
-// chosen so that small clouds still spread over the SMs): shared-memory atomics rank a
+// CTAs (one per SM) walk tiles of up to kBinTile keys (their length chosen so
+// that every CTA gets the same number of tiles): shared-memory atomics rank a
 // tile's keys per bucket, one atomicAdd on the bucket's cursor reserves each
 // bucket's run, the keys are staged in bucket order and leave bucket by
 // bucket, so the runs that consecutive tiles write into a bucket lie next to
@@ -128,7 +128,7 @@ template <bool FROM_POINTS>
 __global__ void __launch_bounds__(kBinThreads, kBinCtasPerSm)
     lsort_bin_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, int n,
                      float min_coord, float range, const char* __restrict__ blob, LcdfLayout L,
-                     int nb, uint32_t cap, int items, uint32_t* __restrict__ cursor,
+                     int nb, uint32_t cap, int tile, uint32_t* __restrict__ cursor,
                      uint32_t* __restrict__ bkeys, uint32_t* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint32_t warp_tot[32];
@@ -145,7 +145,8 @@ __global__ void __launch_bounds__(kBinThreads, kBinCtasPerSm)
   const BucketLookup q = load_lookup(blob, L, nb, s_bounds, s_coarse);
   const float scale = __fdiv_rn(1024.0f, range);
   const int tid = threadIdx.x;
-  const int tile = kBinThreads * items;  // items in [1, kBinItems]
+  // tile in [1, kBinTile]: thread tid takes positions it * kBinThreads + tid
+  // of its tile; those below the tile's end are a prefix of each warp
   const int tiles = (n + tile - 1) / tile;
   const int per = (nb + kBinThreads - 1) / kBinThreads;  // buckets per thread in the scan
   bool bad = false;
@@ -153,6 +154,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinCtasPerSm)
     for (int b = tid; b < nb; b += kBinThreads) s_cnt[b] = 0;
     __syncthreads();
     const int t0 = t * tile;
+    const int t_end = min(n, t0 + tile);
     uint32_t code[kBinItems], br[kBinItems];  // code; bucket << 16 | rank in the bucket
 #pragma unroll
     for (int h = 0; h < kBinItems; h += 4) {
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinCtasPerSm)
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int i = t0 + (h + u) * kBinThreads + tid;
-        const bool in = h + u < items && i < n;
+        const bool in = i < t_end;
         if (FROM_POINTS) {
           if (in) p[u] = ld_stream_f4(pts + i);
         } else {
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinCtasPerSm)
         const int i = t0 + (h + u) * kBinThreads + tid;
         code[h + u] = 0;
         br[h + u] = 0;
-        if (h + u < items && i < n) {
+        if (i < t_end) {
           uint32_t c;
           if (FROM_POINTS) {
             bool ok;
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinCtasPerSm)
         // (scan-ordered clouds) shrink before the buckets see them. Lanes
         // hold consecutive keys and the valid ones are a prefix of the warp.
         const uint32_t prev = __shfl_up_sync(0xffffffffu, code[h + u], 1);
-        if (h + u < items && i < n && ((tid & 31) == 0 || prev != code[h + u])) {
+        if (i < t_end && ((tid & 31) == 0 || prev != code[h + u])) {
           const uint32_t b = bucket_of(q, code[h + u]);
           br[h + u] = (b << 16) | atomicAdd(&s_cnt[b], 1u) | 0x8000u;  // bit 15: placed
         }
@@ -994,22 +996,23 @@ cudaError_t launch_lsort(const float4* pts, uint32_t* keys, int n, float min_coo
   e = cudaMemsetAsync(ws, 0, p.zero_bytes, s);
   if (e != cudaSuccess) return e;
   mark(rec, s);
-  // kBinCtasPerSm CTAs per SM; tiles of kBinThreads x items keys, items as
-  // large as keeps every CTA busy (kBinItems for large clouds, 1 for
-  // frame-sized ones)
+  // kBinCtasPerSm CTAs per SM, each taking the same number of tiles (rounds)
+  // of at most kBinTile keys: small clouds spread over every SM, large ones
+  // leave no partial last round
   const int sms = device_sm_count() * kBinCtasPerSm;
-  const int items =
-      std::max(1, std::min(kBinItems, (int)(((long long)n + (long long)sms * kBinThreads - 1) /
-                                            ((long long)sms * kBinThreads))));
-  const int tiles = (n + kBinThreads * items - 1) / (kBinThreads * items);
+  const long long per_round = (long long)sms * kBinTile;
+  const int rounds = (int)std::max(1LL, ((long long)n + per_round - 1) / per_round);
+  const long long slots = (long long)sms * rounds;
+  const int tile = (int)std::max(1LL, ((long long)n + slots - 1) / slots);
+  const int tiles = (n + tile - 1) / tile;
   const int grid = std::min(sms, tiles);
   if (pts)
     lsort_bin_kernel<true><<<grid, kBinThreads, bsm, s>>>(pts, keys, n, min_coord, range, blob, p.L,
-                                                          p.nb, p.cap, items, cursor, bkeys,
+                                                          p.nb, p.cap, tile, cursor, bkeys,
                                                           status);
   else
     lsort_bin_kernel<false><<<grid, kBinThreads, bsm, s>>>(nullptr, keys, n, 0.f, 1.f, blob, p.L,
-                                                           p.nb, p.cap, items, cursor, bkeys,
+                                                           p.nb, p.cap, tile, cursor, bkeys,
                                                            status);
   mark(rec, s);
   lsort_bin_stats_kernel<<<1, 1024, 0, s>>>(cursor, p.nb, n, p.cap, threshold, blob, starts, counts,

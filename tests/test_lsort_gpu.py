@@ -58,9 +58,10 @@ def test_lsort_unique_exact(kind, n):
 
 @pytest.mark.parametrize("n", [1023, 1025, 155_649, 466_945, 1_089_537, 1_245_185, 2_000_001])
 def test_lsort_unique_tile_shapes(n):
-    """The one-pass bin sizes its tiles to the input (1,024 to 16,384 keys so
-    that every SM gets tiles): sizes around those steps, with partial last
-    tiles and runs of equal keys (which the bin leaves out of the buckets)."""
+    """The one-pass bin sizes its tiles to the input (up to 16,384 keys, any
+    length, the same number per SM): sizes below and around those steps, with
+    partial last tiles and runs of equal keys (which the bin leaves out of
+    the buckets)."""
     from pipeline_gb300.pipeline import lsort_unique
 
     rng = np.random.default_rng(n)
