@@ -1025,18 +1025,16 @@ def run_sharded_batched(args, rank, world, local_rank):
     import torch.distributed as dist
 
     from pipeline_gb300 import datasets
-    from pipeline_gb300.batch import BatchOctreeBuilder, shard_clouds
+    from pipeline_gb300.batch import ShardBuilder
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     clouds = datasets.batched(512, seed=11)
     sizes = [len(c) for c in clouds]
-    mine = shard_clouds(sizes, world)[rank]
-    pts = torch.from_numpy(np.concatenate([clouds[c] for c in mine], 0)).to(dev)
-    mins = torch.zeros(len(mine), dtype=torch.float32, device=dev)
-    ranges = torch.full((len(mine),), RANGE, dtype=torch.float32, device=dev)
-    b = BatchOctreeBuilder([sizes[c] for c in mine], device=dev)
-    b.capture(pts, mins, ranges)
+    shard = ShardBuilder(sizes, rank, world, device=dev)
+    mine = shard.clouds
+    b = shard
+    b.capture(clouds, [0.0] * len(sizes), [RANGE] * len(sizes))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     for _ in range(max(args.warmup, 3)):
@@ -1061,8 +1059,8 @@ def run_sharded_batched(args, rank, world, local_rank):
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    st = b.cloud_counts()[:, 3]
-    if int(np.bitwise_or.reduce(st.astype(np.int64))) != 0:
+    st = np.array([v[3] for v in b.cloud_counts().values()] or [0], np.int64)
+    if int(np.bitwise_or.reduce(st)) != 0:
         raise RuntimeError("device status set")
     total = int(sum(sizes))
     if rank == 0:

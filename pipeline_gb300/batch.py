@@ -4,7 +4,7 @@
 offsets, workspace), then ``build(points, mins, ranges)`` builds every cloud;
 ``capture()``/``replay()`` run the same launches as one CUDA graph.
 ``shard_clouds`` splits a batch over ranks (independent clouds: no
-collective is needed).
+collective is needed) and ``ShardBuilder`` builds one rank's share of it.
 """
 from __future__ import annotations
 
@@ -29,6 +29,30 @@ def shard_clouds(sizes, world: int) -> list[list[int]]:
         out[r].append(c)
         loads[r] += int(sizes[c])
     return [sorted(x) for x in out]
+
+
+def shard_slices(sizes, clouds) -> list[tuple[int, int]]:
+    """Row ranges [lo, hi) of the given clouds in the batch's concatenated
+    points (clouds stored one after another in index order), in the order
+    the clouds are listed."""
+    start = np.concatenate([[0], np.cumsum(np.asarray(sizes, np.int64))])
+    return [(int(start[c]), int(start[c + 1])) for c in clouds]
+
+
+def pack_shard(points, mins, ranges, sizes, clouds):
+    """The listed clouds' points packed one after another, and their mins and
+    ranges. `points` is the whole batch's (N x 4) float32 tensor or a list of
+    per-cloud arrays; `mins` and `ranges` hold one value per cloud of the
+    batch. Runs on whichever device the inputs are on."""
+    if isinstance(points, (list, tuple)):
+        parts = [torch.as_tensor(points[c]) for c in clouds]
+    else:
+        parts = [points[lo:hi] for lo, hi in shard_slices(sizes, clouds)]
+    mins = torch.as_tensor(mins, dtype=torch.float32)
+    ranges = torch.as_tensor(ranges, dtype=torch.float32)
+    idx = torch.as_tensor(list(clouds), dtype=torch.long, device=mins.device)
+    pts = torch.cat(parts, 0) if parts else torch.zeros((0, 4), dtype=torch.float32)
+    return pts, mins.index_select(0, idx), ranges.index_select(0, idx.to(ranges.device))
 
 
 class BatchOctreeBuilder:
@@ -166,3 +190,69 @@ class BatchOctreeBuilder:
             out[name] = getattr(self, name)[cs:cs + b].cpu().numpy()
         out["oct_nodes"] = oct_nodes_to_numpy(self.nodes[ns:ns + m]) if m else np.zeros(0)
         return out
+
+
+class ShardBuilder:
+    """One rank's share of a batch split over `world` ranks by shard_clouds:
+    the rank builds only its own clouds, as one batched build on its device,
+    with no collective on the data path (the clouds are independent). Cloud
+    indices (`clouds`, `cloud_result`) are the whole batch's."""
+
+    def __init__(self, sizes, rank: int, world: int, device="cuda", model=None, n_buckets=None):
+        if world < 1 or not 0 <= rank < world:
+            raise ValueError("rank must lie in [0, world)")
+        self.sizes = [int(v) for v in sizes]
+        self.rank, self.world = rank, world
+        self.clouds = shard_clouds(self.sizes, world)[rank]
+        self._local = {c: k for k, c in enumerate(self.clouds)}
+        self.n_points = sum(self.sizes[c] for c in self.clouds)
+        self.device = torch.device(device)
+        self.builder = None
+        if self.clouds:
+            self.builder = BatchOctreeBuilder([self.sizes[c] for c in self.clouds], device=device,
+                                              model=model, n_buckets=n_buckets)
+        self._inputs = None
+
+    def select(self, points, mins, ranges):
+        """This rank's points, mins and ranges out of the whole batch's,
+        packed on the rank's device (a 1 x 4 zero tensor stands in for
+        points when the rank's clouds are all empty)."""
+        pts, mn, rg = pack_shard(points, mins, ranges, self.sizes, self.clouds)
+        if pts.shape[0] == 0:
+            pts = torch.zeros((1, 4), dtype=torch.float32)
+        dev = self.device
+        return (pts.to(dev, torch.float32).contiguous(), mn.to(dev).contiguous(),
+                rg.to(dev).contiguous())
+
+    def build(self, points, mins, ranges, stream: torch.cuda.Stream | None = None) -> None:
+        """Build this rank's clouds of the batch (whole-batch inputs, see
+        `select`). A rank without clouds does nothing."""
+        if self.builder is None:
+            return
+        self._inputs = self.select(points, mins, ranges)  # alive while the build runs
+        self.builder.build(*self._inputs, stream=stream)
+
+    def capture(self, points, mins, ranges):
+        """Capture this rank's build in a CUDA graph (inputs packed once and
+        kept for the replays); None for a rank without clouds."""
+        if self.builder is None:
+            return None
+        self._inputs = self.select(points, mins, ranges)
+        return self.builder.capture(*self._inputs)
+
+    def replay(self):
+        if self.builder is not None:
+            self.builder.replay()
+
+    def cloud_counts(self) -> dict:
+        """(U, B, M, status) of each of this rank's clouds, by batch index."""
+        if self.builder is None:
+            return {}
+        cnt = self.builder.cloud_counts()
+        return {c: tuple(int(v) for v in cnt[k]) for c, k in self._local.items()}
+
+    def cloud_result(self, c: int) -> dict:
+        """Every stage buffer of batch cloud `c`, which must be on this rank."""
+        if c not in self._local:
+            raise ValueError(f"cloud {c} is not on rank {self.rank}")
+        return self.builder.cloud_result(self._local[c])

@@ -1,9 +1,9 @@
 """The batched build split over two ranks, each building its shard on the GPU.
 
 Two processes (gloo for the host-side gather; both on cuda:0, whose kernels
-never wait on each other) take their clouds with shard_clouds, build them in
-one batched build each, and all-gather per-cloud hashes of every stage
-buffer. Together they must cover every cloud exactly once, and every cloud
+never wait on each other) each build their clouds (ShardBuilder: the clouds
+shard_clouds gives the rank, in one batched build) and all-gather per-cloud
+hashes of every stage buffer. Together they must cover every cloud exactly once, and every cloud
 must equal the oracle's build of it (apps/cpu_demo/main.cpp:72-154)."""
 import os
 import socket
@@ -37,21 +37,17 @@ def _worker(rank, world, port, out):
     import torch.distributed as dist
 
     from oracle import oracle as O
-    from pipeline_gb300.batch import BatchOctreeBuilder, shard_clouds
+    from pipeline_gb300.batch import ShardBuilder
 
     dist.init_process_group("gloo", rank=rank, world_size=world)
     clouds = _clouds()
     sizes = [len(c) for c in clouds]
-    mine = shard_clouds(sizes, world)[rank]
-    b = BatchOctreeBuilder([sizes[c] for c in mine], device="cuda:0")
-    pts = torch.from_numpy(np.concatenate([clouds[c] for c in mine], 0)).cuda()
-    mins = torch.zeros(len(mine), dtype=torch.float32, device="cuda")
-    ranges = torch.full((len(mine),), 1024.0, dtype=torch.float32, device="cuda")
-    b.build(pts, mins, ranges)
-    counts = b.cloud_counts()
+    shard = ShardBuilder(sizes, rank, world, device="cuda:0")
+    shard.build(clouds, [0.0] * len(sizes), [1024.0] * len(sizes))
+    torch.cuda.synchronize()
     hashes = {}
-    for j, c in enumerate(mine):
-        r = b.cloud_result(j, counts)
+    for c in shard.clouds:
+        r = shard.cloud_result(c)
         hashes[c] = (r["n_unique"], r["n_oct"], r["status"],
                      [O.fnv1a64(np.asarray(r[k])) for k in STAGES])
     gathered = [None] * world
