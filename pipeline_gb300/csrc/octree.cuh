@@ -136,7 +136,10 @@ __device__ __forceinline__ void emit_node(int mode, int i, const OctArgs& a, con
         }
       }
     }
-    const int dst = a.offsets[rn];
+    // rn == i with octree nodes: its offset is already in base (a load here
+    // would wait behind the MakeOctNodes atomics, which the compiler may not
+    // move it above).
+    const int dst = (make && rn == i) ? base : a.offsets[rn];
     const uint32_t sh = (uint32_t)(30 - 3 * (L + 1)) & 31u;
     if (!lc_ok) {
       raise_status(status, kStatusWalkLimit);
