@@ -23,6 +23,24 @@ constexpr uint32_t kWaitPollCap = 1u << 26;
 
 constexpr int kWarp = 32;
 
+// Programmatic dependent launch. A kernel launched by launch_chained (host
+// side, kernels.cuh) may have its CTAs scheduled while the kernel before it
+// on the stream is still finishing; chain_wait() blocks until that kernel has
+// completed and its writes are visible (for a kernel launched without the
+// attribute it returns at once). Every kernel that launch_chained launches
+// calls chain_wait() before its first global-memory access, then
+// chain_release(), which lets the next kernel's CTAs be scheduled once all of
+// this kernel's CTAs have started: so at most one waiting grid sits beside a
+// running one, and no running grid ever lacks the slots its later CTAs need.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void chain_enter() {
+  chain_wait();
+  chain_release();
+}
+
 __device__ __forceinline__ uint32_t lane_id() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));

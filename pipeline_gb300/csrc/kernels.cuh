@@ -32,6 +32,31 @@ static inline void mark(Recorder* r, cudaStream_t s) {
 // SM count of the current device (cached per device).
 int device_sm_count();
 
+// Whether launch_chained sets the programmatic-serialization attribute: on
+// unless the environment sets OCT_PDL=0 (read once per process).
+bool chained_launches();
+
+// Launch of a kernel whose body starts with chain_enter() (common.cuh), with
+// programmatic stream serialization: its CTAs may be scheduled during the
+// tail of the previous kernel on the stream and wait there on the device, so
+// consecutive kernels (and their CUDA-graph replays) do not pay a full launch
+// gap. Results are the same as a plain launch's.
+template <typename... P, typename... A>
+static inline cudaError_t launch_chained(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
+                                         cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t c = {};
+  c.gridDim = grid;
+  c.blockDim = block;
+  c.dynamicSmemBytes = smem;
+  c.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  c.attrs = at;
+  c.numAttrs = chained_launches() ? 1 : 0;
+  return cudaLaunchKernelEx(&c, kernel, static_cast<P>(args)...);
+}
+
 // Raises func's dynamic shared-memory limit to at least `bytes` on the
 // current device (once per device and kernel; kernel attributes are per
 // device context).

@@ -47,6 +47,7 @@ size_t msd_scratch_bytes() { return sizeof(uint32_t) * (3 * (size_t)kMsdBuckets 
 
 __global__ void __launch_bounds__(kMsdBuckets)
     msd_gate_kernel(const uint32_t* __restrict__ top_hist, int n, uint32_t* __restrict__ flags) {
+  chain_enter();
   __shared__ uint32_t s_max[kMsdBuckets / 32];
   const uint32_t m = __reduce_max_sync(0xffffffffu, top_hist[threadIdx.x]);
   if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
@@ -173,6 +174,7 @@ __global__ void __launch_bounds__(kMsdThreads, 1)
     msd_bucket_kernel(uint32_t* __restrict__ keys, const uint32_t* __restrict__ top_base,
                       const uint32_t* __restrict__ top_hist, uint32_t* __restrict__ ucount,
                       const uint32_t* __restrict__ gate, uint32_t* __restrict__ status) {
+  chain_enter();
   if (*gate == 0) return;
   extern __shared__ uint4 s_bm4[];
   uint32_t* bm = reinterpret_cast<uint32_t*>(s_bm4);
@@ -191,6 +193,7 @@ __global__ void __launch_bounds__(kMsdBuckets)
                          int* __restrict__ next_start, const uint32_t* __restrict__ top_base,
                          int* __restrict__ d_unique, TreeScratch S,
                          const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (*gate == 0) return;
   __shared__ uint32_t warp_tot[32];
   __shared__ uint32_t total;
@@ -295,6 +298,7 @@ __global__ void __launch_bounds__(kPackThreads)
                     const uint32_t* __restrict__ ucount, const uint32_t* __restrict__ uoff,
                     const int* __restrict__ next_start, uint32_t* __restrict__ codes,
                     TreeScratch S, const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (*gate == 0) return;
   __shared__ uint32_t s_tmin[kPackTiles];
   const int tid = threadIdx.x;
@@ -307,8 +311,7 @@ __global__ void __launch_bounds__(kPackThreads)
 }
 
 cudaError_t launch_msd_gate(const uint32_t* top_hist, int n, uint32_t* flags, cudaStream_t s) {
-  msd_gate_kernel<<<1, kMsdBuckets, 0, s>>>(top_hist, n, flags);
-  return cudaGetLastError();
+  return launch_chained(msd_gate_kernel, dim3(1), dim3(kMsdBuckets), 0, s, top_hist, n, flags);
 }
 
 cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const uint32_t* top_hist,
@@ -319,8 +322,8 @@ cudaError_t launch_msd_buckets(uint32_t* keys, const uint32_t* top_base, const u
   if (e != cudaSuccess) return e;
   uint32_t* ucount = static_cast<uint32_t*>(scratch);
   const int grid = std::min(kMsdBuckets, device_sm_count());  // one CTA fits an SM
-  msd_bucket_kernel<<<grid, kMsdThreads, smem, s>>>(keys, top_base, top_hist, ucount, gate, status);
-  return cudaGetLastError();
+  return launch_chained(msd_bucket_kernel, dim3(grid), dim3(kMsdThreads), smem, s, keys, top_base,
+                        top_hist, ucount, gate, status);
 }
 
 cudaError_t launch_msd_pack(const uint32_t* keys, const uint32_t* top_base, int n,
@@ -330,13 +333,11 @@ cudaError_t launch_msd_pack(const uint32_t* keys, const uint32_t* top_base, int 
   uint32_t* uoff = ucount + kMsdBuckets;
   int* next_start = reinterpret_cast<int*>(uoff + kMsdBuckets + 1);
   const TreeScratch S = tree_scratch_carve(tree_scratch, n);
-  msd_pack_scan_kernel<<<1, kMsdBuckets, 0, s>>>(ucount, uoff, next_start, top_base, d_unique, S,
-                                                 gate);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_chained(msd_pack_scan_kernel, dim3(1), dim3(kMsdBuckets), 0, s, ucount,
+                                 uoff, next_start, top_base, d_unique, S, gate);
   if (e != cudaSuccess) return e;
-  msd_pack_kernel<<<kMsdBuckets, kPackThreads, 0, s>>>(keys, top_base, ucount, uoff, next_start,
-                                                       codes_out, S, gate);
-  return cudaGetLastError();
+  return launch_chained(msd_pack_kernel, dim3(kMsdBuckets), dim3(kPackThreads), 0, s, keys,
+                        top_base, ucount, uoff, next_start, codes_out, S, gate);
 }
 
 }  // namespace octgb

@@ -23,6 +23,8 @@
 // Sequence tags (32-bit, larger = later):
 //   MakeOctNodes step j of node i : ((i << 4) | j) + 1        (i < 2^27)
 //   LinkLeafNodes side s of node i: 0x80000000 | (i << 1) | s
+#include <algorithm>
+
 #include "octree.cuh"
 
 namespace octgb {
@@ -47,6 +49,7 @@ OctTags oct_tags_carve(void* base, int cap) {
 
 __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
                                                        uint32_t* __restrict__ status) {
+  chain_enter();
   const Sizes z = read_sizes(a);
   if (!z.fits) {
     if (blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, kStatusCapacity);
@@ -60,6 +63,7 @@ __global__ void __launch_bounds__(256) oct_zero_kernel(OctArgs a, OctTags t,
 __global__ void __launch_bounds__(256, 8) oct_emit_kernel(int mode, OctArgs a, OctTags t,
                                                        uint32_t* __restrict__ status,
                                                        bool report_capacity) {
+  chain_enter();
   const Sizes z = read_sizes(a);
   if (!z.fits) {
     if (report_capacity && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, kStatusCapacity);
@@ -71,6 +75,7 @@ __global__ void __launch_bounds__(256, 8) oct_emit_kernel(int mode, OctArgs a, O
 }
 
 __global__ void __launch_bounds__(kFinThreads, 8) oct_finalize_kernel(int mode, OctArgs a, OctTags t) {
+  chain_enter();
   __shared__ __align__(16) int s_nodes[kFinThreads * kNodeWords];
   const Sizes z = read_sizes(a);
   if (!z.fits || z.n_brt < 1) return;
@@ -114,28 +119,30 @@ cudaError_t launch_octree(int mode, const OctArgs& a, const OctTags& t, uint32_t
   cudaError_t e;
   if (!tags_clear) {
     const int zgrid = device_sm_count() * 8;
-    oct_zero_kernel<<<zgrid, 256, 0, s>>>(a, t, status);
-    e = cudaGetLastError();
+    e = launch_chained(oct_zero_kernel, dim3(zgrid), dim3(256), 0, s, a, t, status);
     if (e != cudaSuccess) return e;
     mark(rec, s);
   }
   int nb = a.d_unique ? a.n_brt_host : a.n_brt_host;
   int egrid = (nb + 255) / 256;
   if (egrid < 1) egrid = 1;
-  oct_emit_kernel<<<egrid, 256, 0, s>>>(mode, a, t, status, tags_clear);
-  e = cudaGetLastError();
+  e = launch_chained(oct_emit_kernel, dim3(egrid), dim3(256), 0, s, mode, a, t, status, tags_clear);
   if (e != cudaSuccess) return e;
   mark(rec, s);
+  // One wave at 8 CTAs per SM, each walking the 256-slot blocks: the node
+  // count is known only on the device, and a grid sized by the capacity would
+  // leave its CTAs past the last node to start, wait and exit in the tail.
   int fgrid = (a.cap + kFinThreads - 1) / kFinThreads;
+  fgrid = std::min(fgrid, device_sm_count() * 8);
   if (fgrid < 1) fgrid = 1;
-  oct_finalize_kernel<<<fgrid, kFinThreads, 0, s>>>(mode, a, t);
-  e = cudaGetLastError();
+  e = launch_chained(oct_finalize_kernel, dim3(fgrid), dim3(kFinThreads), 0, s, mode, a, t);
   if (e == cudaSuccess) mark(rec, s);
   return e;
 }
 
 __global__ void publish_counts_kernel(const int* d_unique, const int* d_max_slot,
                                       const uint32_t* status, int* out) {
+  chain_enter();
   const int u = *d_unique;
   const int b = max(u - 1, 0);
   out[0] = u;
@@ -146,8 +153,8 @@ __global__ void publish_counts_kernel(const int* d_unique, const int* d_max_slot
 
 cudaError_t launch_publish_counts(const int* d_unique, const int* d_max_slot,
                                   const uint32_t* status, int* out, cudaStream_t s) {
-  publish_counts_kernel<<<1, 1, 0, s>>>(d_unique, d_max_slot, status, out);
-  return cudaGetLastError();
+  return launch_chained(publish_counts_kernel, dim3(1), dim3(1), 0, s, d_unique, d_max_slot, status,
+                        out);
 }
 
 }  // namespace octgb

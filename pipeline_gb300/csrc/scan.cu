@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(kUqThreads)
     unique_kernel(const uint32_t* src, uint32_t* dst, int n, int* __restrict__ d_count,
                   unsigned long long* __restrict__ lb, uint32_t* __restrict__ counter, int tiles,
                   uint32_t* __restrict__ status, const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   __shared__ uint32_t s_keys[kUqTile + kUqTile / 32];
   __shared__ uint32_t s_warp[32];
@@ -162,10 +163,10 @@ cudaError_t launch_unique_gated(const uint32_t* src, uint32_t* dst, int n, int* 
                                 const uint32_t* gate, cudaStream_t s) {
   if (n <= 0) return gate ? cudaSuccess : cudaMemsetAsync(d_count, 0, sizeof(int), s);
   char* c = static_cast<char*>(ctrl);
-  unique_kernel<<<plan->tiles, kUqThreads, 0, s>>>(
-      src, dst, n, d_count, reinterpret_cast<unsigned long long*>(c + plan->lookback_off),
-      reinterpret_cast<uint32_t*>(c + plan->counter_off), plan->tiles, status, gate);
-  return cudaGetLastError();
+  return launch_chained(unique_kernel, dim3(plan->tiles), dim3(kUqThreads), 0, s, src, dst, n,
+                        d_count, reinterpret_cast<unsigned long long*>(c + plan->lookback_off),
+                        reinterpret_cast<uint32_t*>(c + plan->counter_off), plan->tiles, status,
+                        gate);
 }
 
 cudaError_t launch_unique(const uint32_t* src, uint32_t* dst, int n, int* d_count,
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(kEsThreads)
                      unsigned long long* __restrict__ lb, uint32_t* __restrict__ counter,
                      uint32_t* __restrict__ status, OctTags zt,
                      const uint32_t* __restrict__ tile_prefix) {
+  chain_enter();
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_misc[4];
   __shared__ int s_max[kEsThreads / 32];
@@ -362,10 +364,9 @@ cudaError_t launch_edge_scan(int mode, int n_host, const int* d_unique, const ui
       c ? reinterpret_cast<unsigned long long*>(c + plan->lookback_off) : nullptr;
   uint32_t* counter = c ? reinterpret_cast<uint32_t*>(c + plan->counter_off) : nullptr;
   if (mode != kEdgeOnly && !c) return cudaErrorInvalidValue;
-  edge_scan_kernel<<<plan->tiles, kEsThreads, 0, s>>>(mode, n_host, d_unique, prefix_n, parent,
-                                                      ec, ps, d_max_slot, lb, counter, status,
-                                                      OctTags{}, nullptr);
-  return cudaGetLastError();
+  return launch_chained(edge_scan_kernel, dim3(plan->tiles), dim3(kEsThreads), 0, s, mode, n_host,
+                        d_unique, prefix_n, parent, ec, ps, d_max_slot, lb, counter, status,
+                        OctTags{}, nullptr);
 }
 
 // Exclusive scan of the per-tile edge-count sums (one CTA).
@@ -374,6 +375,7 @@ __global__ void __launch_bounds__(kTsThreads)
     tile_sums_scan_kernel(int tiles_fixed, int n_host, const int* __restrict__ d_unique,
                           const int* __restrict__ tile_sum, uint32_t* __restrict__ tile_prefix,
                           int* __restrict__ total_out, const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
@@ -397,15 +399,13 @@ cudaError_t launch_prefix_sum_clear_tags(int n_host, const int* d_unique, int* e
   static_assert(kEsTile == 4096, "scan tiles are the radix-tree tiles");
   if (n_host <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve(tree_scratch, n_host);
-  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(0, n_host, d_unique, S.tile_sum, S.tile_prefix,
-                                                 nullptr, nullptr);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_chained(tile_sums_scan_kernel, dim3(1), dim3(kTsThreads), 0, s, 0, n_host,
+                                 d_unique, S.tile_sum, S.tile_prefix, nullptr, nullptr);
   if (e != cudaSuccess) return e;
   const int tiles = (n_host + kEsTile - 1) / kEsTile;
-  edge_scan_kernel<<<tiles, kEsThreads, 0, s>>>(kScanOnly, n_host, d_unique, nullptr, nullptr, ec,
-                                                ps, d_max_slot, nullptr, nullptr, status,
-                                                tags.cap > 0 ? tags : OctTags{}, S.tile_prefix);
-  return cudaGetLastError();
+  return launch_chained(edge_scan_kernel, dim3(tiles), dim3(kEsThreads), 0, s, kScanOnly, n_host,
+                        d_unique, nullptr, nullptr, ec, ps, d_max_slot, nullptr, nullptr, status,
+                        tags.cap > 0 ? tags : OctTags{}, S.tile_prefix);
 }
 
 __global__ void __launch_bounds__(256)
@@ -413,6 +413,7 @@ __global__ void __launch_bounds__(256)
                       const uint32_t* __restrict__ codes, uint8_t* __restrict__ prefix_n,
                       uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
                       int* __restrict__ left_child, int* __restrict__ parent) {
+  chain_enter();
   const int n = d_unique ? max(*d_unique - 1, 0) : n_host;
   const int stride = gridDim.x * blockDim.x;
   const GlobalCodes gc{codes};
@@ -425,25 +426,22 @@ cudaError_t launch_radix_tree(int n_host, const int* d_unique, const uint32_t* c
                               int* parent, cudaStream_t s) {
   if (n_host <= 0) return cudaSuccess;
   const int grid = (n_host + 255) / 256;
-  radix_tree_kernel<<<grid, 256, 0, s>>>(n_host, d_unique, codes, prefix_n, hll, hlr,
-                                         left_child, parent);
-  return cudaGetLastError();
+  return launch_chained(radix_tree_kernel, dim3(grid), dim3(256), 0, s, n_host, d_unique, codes,
+                        prefix_n, hll, hlr, left_child, parent);
 }
 
 cudaError_t launch_tile_sums_scan(int tiles, const int* tile_sum, uint32_t* tile_prefix,
                                   cudaStream_t s) {
   if (tiles <= 0) return cudaSuccess;
-  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(tiles, 0, nullptr, tile_sum, tile_prefix,
-                                                 nullptr, nullptr);
-  return cudaGetLastError();
+  return launch_chained(tile_sums_scan_kernel, dim3(1), dim3(kTsThreads), 0, s, tiles, 0, nullptr,
+                        tile_sum, tile_prefix, nullptr, nullptr);
 }
 
 cudaError_t launch_tile_counts_scan(int tiles, const int* counts, uint32_t* prefix,
                                     int* total_out, cudaStream_t s, const uint32_t* gate) {
   if (tiles <= 0) return cudaSuccess;
-  tile_sums_scan_kernel<<<1, kTsThreads, 0, s>>>(tiles, 0, nullptr, counts, prefix, total_out,
-                                                 gate);
-  return cudaGetLastError();
+  return launch_chained(tile_sums_scan_kernel, dim3(1), dim3(kTsThreads), 0, s, tiles, 0, nullptr,
+                        counts, prefix, total_out, gate);
 }
 
 }  // namespace octgb

@@ -15,6 +15,7 @@
 // 30-bit Morton keys take 3 passes of 10-bit digits (28 B/key of HBM traffic
 // including the histogram read) instead of the reference's 4 passes of 8.
 #include <atomic>
+#include <cstdlib>
 #include <mutex>
 #include <tuple>
 #include <vector>
@@ -31,6 +32,7 @@ __global__ void __launch_bounds__(256)
     morton_kernel(const float4* __restrict__ pts, uint32_t* __restrict__ keys, long long n,
                   float min_coord, float range, uint32_t* __restrict__ ghist, int passes,
                   uint32_t* __restrict__ status) {
+  chain_enter();
   constexpr int BINS = 1 << RB;
   constexpr int PASSES = (30 + RB - 1) / RB;  // the plan's passes over 30-bit codes
   extern __shared__ uint32_t s_hist[];  // [PASSES * BINS] histograms, then the spread table
@@ -88,6 +90,7 @@ template <int RB>
 __global__ void __launch_bounds__(256)
     histogram_kernel(const uint32_t* __restrict__ keys, int n, uint32_t* __restrict__ ghist,
                      int passes, const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   constexpr int BINS = 1 << RB;
   extern __shared__ uint32_t s_hist[];
@@ -119,6 +122,7 @@ template <int RB>
 __global__ void __launch_bounds__(1024) hist_scan_kernel(const uint32_t* __restrict__ ghist,
                                                          uint32_t* __restrict__ base,
                                                          const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   constexpr int BINS = 1 << RB;
   constexpr int T = BINS < 1024 ? BINS : 1024;
@@ -251,6 +255,7 @@ __global__ void __launch_bounds__(WARPS * 32, (ITEMS <= 16 ? 2 : 1))
                      const uint32_t* __restrict__ tile_prefix, uint32_t* __restrict__ status,
                      const uint32_t* __restrict__ gate, const int4* __restrict__ tdesc,
                      DigitAlt alt) {
+  chain_enter();
   if (gate && *gate == 0) return;
   // The MSD form's top-digit scatter: the order inside a bucket is free, so a
   // tile takes its digit runs' places with one atomic add per digit on the
@@ -452,6 +457,7 @@ __global__ void __launch_bounds__(256)
     tile_hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tile_keys,
                      uint32_t* __restrict__ th, const uint32_t* __restrict__ gate,
                      const int4* __restrict__ tdesc, uint32_t* __restrict__ part, int tiles) {
+  chain_enter();
   if (gate && *gate == 0) return;
   constexpr int BINS = 1 << RB;
   __shared__ uint32_t h[BINS];
@@ -500,6 +506,7 @@ __global__ void __launch_bounds__(1024)
     tile_scan_split_kernel(uint32_t* __restrict__ th, int tiles, int bins,
                            const uint32_t* __restrict__ bin_base, const uint32_t* __restrict__ part,
                            const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   __shared__ uint32_t sums[32][33];
   const int l = threadIdx.x & 31, g = threadIdx.x >> 5;
@@ -602,6 +609,14 @@ int device_sm_count() {
   return v;
 }
 
+bool chained_launches() {
+  static const bool on = [] {
+    const char* v = std::getenv("OCT_PDL");
+    return !(v && v[0] == '0' && v[1] == '\0');
+  }();
+  return on;
+}
+
 cudaError_t set_smem_limit(const void* func, int bytes) {
   const int dev = current_device();
   std::lock_guard<std::mutex> lock(g_attr_mu);
@@ -638,9 +653,8 @@ static cudaError_t launch_pass_t(const uint32_t* src, uint32_t* dst, int n, int 
   const cudaError_t ea = set_smem_limit(reinterpret_cast<const void*>(k), L::BYTES);
   if (ea != cudaSuccess) return ea;
   const int tiles = tiles_override > 0 ? tiles_override : (n + L::TILE - 1) / L::TILE;
-  k<<<tiles, WARPS * 32, L::BYTES, s>>>(src, dst, n, shift, base, lookback, counter, tile_prefix,
-                                        status, gate, tdesc, alt);
-  return cudaGetLastError();
+  return launch_chained(k, dim3(tiles), dim3(WARPS * 32), L::BYTES, s, src, dst, n, shift, base,
+                        lookback, counter, tile_prefix, status, gate, tdesc, alt);
 }
 
 template <int RB, int WARPS, int ITEMS>
@@ -691,16 +705,13 @@ cudaError_t launch_morton(const float4* pts, uint32_t* keys, long long n, float 
     uint32_t* hist = reinterpret_cast<uint32_t*>(static_cast<char*>(ctrl) + plan->hist_off);
     const size_t sm = sizeof(uint32_t) * (plan->passes * plan->bins + 1024);
     if (plan->radix_bits == 10)
-      morton_kernel<10, true><<<grid, 256, sm, s>>>(pts, keys, n, min_coord, range, hist,
-                                                    plan->passes, status);
-    else
-      morton_kernel<8, true><<<grid, 256, sm, s>>>(pts, keys, n, min_coord, range, hist,
-                                                   plan->passes, status);
-  } else {
-    morton_kernel<10, false><<<grid, 256, sizeof(uint32_t) * 1024, s>>>(pts, keys, n, min_coord,
-                                                                        range, nullptr, 0, status);
+      return launch_chained(morton_kernel<10, true>, dim3(grid), dim3(256), sm, s, pts, keys, n,
+                            min_coord, range, hist, plan->passes, status);
+    return launch_chained(morton_kernel<8, true>, dim3(grid), dim3(256), sm, s, pts, keys, n,
+                          min_coord, range, hist, plan->passes, status);
   }
-  return cudaGetLastError();
+  return launch_chained(morton_kernel<10, false>, dim3(grid), dim3(256), sizeof(uint32_t) * 1024, s,
+                        pts, keys, n, min_coord, range, nullptr, 0, status);
 }
 
 cudaError_t launch_histogram_gated(const uint32_t* keys, const SortPlan* plan, void* ctrl,
@@ -712,10 +723,10 @@ cudaError_t launch_histogram_gated(const uint32_t* keys, const SortPlan* plan, v
   int need = (plan->n / 4 + 255) / 256 + 1;
   const int grid = need < blocks ? need : blocks;
   if (plan->radix_bits == 10)
-    histogram_kernel<10><<<grid, 256, sm, s>>>(keys, plan->n, hist, plan->passes, gate);
-  else
-    histogram_kernel<8><<<grid, 256, sm, s>>>(keys, plan->n, hist, plan->passes, gate);
-  return cudaGetLastError();
+    return launch_chained(histogram_kernel<10>, dim3(grid), dim3(256), sm, s, keys, plan->n, hist,
+                          plan->passes, gate);
+  return launch_chained(histogram_kernel<8>, dim3(grid), dim3(256), sm, s, keys, plan->n, hist,
+                        plan->passes, gate);
 }
 
 cudaError_t launch_histogram(const uint32_t* keys, const SortPlan* plan, void* ctrl,
@@ -737,11 +748,11 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
   uint32_t* lookback = reinterpret_cast<uint32_t*>(c + plan->lookback_off);
   uint32_t* th = reinterpret_cast<uint32_t*>(c + plan->tile_hist_off);
   uint32_t* part = reinterpret_cast<uint32_t*>(c + plan->tile_part_off);
-  if (plan->radix_bits == 10)
-    hist_scan_kernel<10><<<plan->passes, 1024, 0, s>>>(hist, base, gate);
-  else
-    hist_scan_kernel<8><<<plan->passes, 256, 0, s>>>(hist, base, gate);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e =
+      plan->radix_bits == 10
+          ? launch_chained(hist_scan_kernel<10>, dim3(plan->passes), dim3(1024), 0, s, hist, base,
+                           gate) : launch_chained(hist_scan_kernel<8>, dim3(plan->passes),
+                           dim3(256), 0, s, hist, base, gate);
   if (e != cudaSuccess) return e;
   mark(rec, s);
   // The MSD form's top-digit scatter reuses pass 0's pass launch (unstable,
@@ -767,14 +778,17 @@ static cudaError_t sort_passes_impl(uint32_t* keys, uint32_t* alt, const SortPla
       // tile histograms and their scan run for the LSD form only
       const uint32_t* gs = (p == 0 && alt0.flag) ? lsd_flag : g;
       uint32_t* pp = part + (size_t)p * kScanSplits * plan->bins;
-      if (plan->radix_bits == 10)
-        tile_hist_kernel<10><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gs,
-                                                         nullptr, pp, plan->tiles);
-      else
-        tile_hist_kernel<8><<<tile_hist_grid(plan->tiles), 256, 0, s>>>(a, plan->n, shift, plan->tile, th, gs,
-                                                        nullptr, pp, plan->tiles);
-      tile_scan_split_kernel<<<dim3((plan->bins + 31) / 32, kScanSplits), 1024, 0, s>>>(
-          th, plan->tiles, plan->bins, base + p * plan->bins, pp, gs);
+      const dim3 hg(tile_hist_grid(plan->tiles));
+      e = plan->radix_bits == 10
+              ? launch_chained(tile_hist_kernel<10>, hg, dim3(256), 0, s, a, plan->n, shift,
+                               plan->tile, th, gs, nullptr, pp,
+                               plan->tiles) : launch_chained(tile_hist_kernel<8>, hg, dim3(256), 0,
+                               s, a, plan->n, shift, plan->tile, th, gs, nullptr, pp, plan->tiles);
+      if (e != cudaSuccess) return e;
+      e = launch_chained(tile_scan_split_kernel, dim3((plan->bins + 31) / 32, kScanSplits),
+                         dim3(1024), 0, s, th, plan->tiles, plan->bins, base + p * plan->bins, pp,
+                         gs);
+      if (e != cudaSuccess) return e;
     }
     uint32_t* lb = lookback + (size_t)p * plan->tiles * plan->bins;
     e = launch_pass(*plan, p > 0, a, b, shift, base + p * plan->bins,
@@ -820,10 +834,10 @@ cudaError_t launch_tile_hist(int radix_bits, const uint32_t* keys, int n, int sh
   // a gated launch walks the tiles from a capped grid (few no-op CTAs)
   const int grid = gate ? tile_hist_grid(tiles) : tiles;
   if (radix_bits == 10)
-    tile_hist_kernel<10><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles);
-  else
-    tile_hist_kernel<8><<<grid, 256, 0, s>>>(keys, n, shift, 0, th, gate, tdesc, nullptr, tiles);
-  return cudaGetLastError();
+    return launch_chained(tile_hist_kernel<10>, dim3(grid), dim3(256), 0, s, keys, n, shift, 0, th,
+                          gate, tdesc, nullptr, tiles);
+  return launch_chained(tile_hist_kernel<8>, dim3(grid), dim3(256), 0, s, keys, n, shift, 0, th,
+                        gate, tdesc, nullptr, tiles);
 }
 
 }  // namespace octgb

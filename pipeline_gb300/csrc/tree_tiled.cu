@@ -160,6 +160,7 @@ __device__ __forceinline__ void value_ballots(uint32_t d, uint32_t (&b)[5]) {
 template <class Map>
 __global__ void __launch_bounds__(kTtAThreads)
     tree_tiles_kernel(Map map, const uint32_t* __restrict__ codes_all, TreeScratch S) {
+  chain_enter();
   constexpr int kWarps = kTtAThreads / 32;
   __shared__ uint32_t s_min[kWarps];
   const TileInfo I = map(blockIdx.x);
@@ -343,6 +344,7 @@ __device__ __forceinline__ void emit_root(const TreeOut& o, int n, int q, uint32
 template <class Map>
 __global__ void __launch_bounds__(kTtBThreads)
     tree_nodes_kernel(Map map, const uint32_t* __restrict__ codes, TreeScratch S, TreeOut o) {
+  chain_enter();
   __shared__ __align__(16) uint8_t s_D[kTtTile];
   __shared__ int16_t s_pl[kTtChunks][32];  // last tile position before the chunk with D < v
   __shared__ int16_t s_sf[kTtChunks][32];  // first tile position after the chunk with D < v
@@ -572,6 +574,7 @@ template <class Map>
 __global__ void __launch_bounds__(kUdThreads)
     unique_count_kernel(const uint32_t* __restrict__ keys, Map map, int n_tiles, TreeScratch S,
                         const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   __shared__ int s_cnt[kUdThreads / 32];
   const int tid = threadIdx.x;
@@ -646,6 +649,7 @@ __global__ void __launch_bounds__(kUdThreads)
     unique_deltas_kernel(const uint32_t* __restrict__ keys, Map map, uint32_t* __restrict__ out,
                          int n_tiles, TreeScratch S, int* __restrict__ unique_c,
                          const uint32_t* __restrict__ gate) {
+  chain_enter();
   if (gate && *gate == 0) return;
   __shared__ uint32_t s_keys[kTtTile + kTtTile / 32];
   __shared__ uint8_t s_d[kTtTile];
@@ -746,14 +750,13 @@ cudaError_t launch_unique_deltas(const uint32_t* sorted, int n, uint32_t* codes_
   if (n <= 0) return cudaMemsetAsync(d_unique, 0, sizeof(int), s);
   const TreeScratch S = tree_scratch_carve(tree_scratch, n);
   const OneKeys map{n};
-  unique_count_kernel<<<unique_grid(S.tiles), kUdThreads, 0, s>>>(sorted, map, S.tiles, S, gate);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_chained(unique_count_kernel<OneKeys>, dim3(unique_grid(S.tiles)),
+                                 dim3(kUdThreads), 0, s, sorted, map, S.tiles, S, gate);
   if (e == cudaSuccess)
     e = launch_tile_counts_scan(S.tiles, S.tile_heads, S.tile_upos, d_unique, s, gate);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<unique_grid(S.tiles), kUdThreads, 0, s>>>(sorted, map, codes_out, S.tiles, S,
-                                                                   nullptr, gate);
-  return cudaGetLastError();
+  return launch_chained(unique_deltas_kernel<OneKeys>, dim3(unique_grid(S.tiles)), dim3(kUdThreads),
+                        0, s, sorted, map, codes_out, S.tiles, S, nullptr, gate);
 }
 
 cudaError_t launch_batch_unique_deltas(const uint32_t* sorted, const int4* tiles, int n_tiles,
@@ -762,13 +765,12 @@ cudaError_t launch_batch_unique_deltas(const uint32_t* sorted, const int4* tiles
   if (n_tiles <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
   const CloudKeys map{tiles, n_tiles, start};
-  unique_count_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, n_tiles, S, nullptr);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_chained(unique_count_kernel<CloudKeys>, dim3(n_tiles), dim3(kUdThreads), 0,
+                                 s, sorted, map, n_tiles, S, nullptr);
   if (e == cudaSuccess) e = launch_tile_counts_scan(n_tiles, S.tile_heads, S.tile_upos, nullptr, s);
   if (e != cudaSuccess) return e;
-  unique_deltas_kernel<<<n_tiles, kUdThreads, 0, s>>>(sorted, map, codes_out, n_tiles, S,
-                                                                   unique_c, nullptr);
-  return cudaGetLastError();
+  return launch_chained(unique_deltas_kernel<CloudKeys>, dim3(n_tiles), dim3(kUdThreads), 0, s,
+                        sorted, map, codes_out, n_tiles, S, unique_c, nullptr);
 }
 
 cudaError_t launch_batch_radix_tree_from_deltas(const int4* tiles, int n_tiles, const int* start,
@@ -780,8 +782,8 @@ cudaError_t launch_batch_radix_tree_from_deltas(const int4* tiles, int n_tiles, 
   const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
   const CloudTiles map{tiles, start, unique_c};
   const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
-  tree_nodes_kernel<<<n_tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
-  return cudaGetLastError();
+  return launch_chained(tree_nodes_kernel<CloudTiles>, dim3(n_tiles), dim3(kTtBThreads), 0, s, map,
+                        codes, S, o);
 }
 
 cudaError_t launch_radix_tree_from_deltas(int n_host, const int* d_unique, const uint32_t* codes,
@@ -792,8 +794,8 @@ cudaError_t launch_radix_tree_from_deltas(int n_host, const int* d_unique, const
   const TreeScratch S = tree_scratch_carve(scratch, n_host);
   const OneCloud map{n_host, d_unique, S.tiles};
   const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
-  tree_nodes_kernel<<<S.tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
-  return cudaGetLastError();
+  return launch_chained(tree_nodes_kernel<OneCloud>, dim3(S.tiles), dim3(kTtBThreads), 0, s, map,
+                        codes, S, o);
 }
 
 cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint32_t* codes,
@@ -803,12 +805,12 @@ cudaError_t launch_radix_tree_sorted(int n_host, const int* d_unique, const uint
   if (n_host <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve(scratch, n_host);
   const OneCloud map{n_host, d_unique, S.tiles};
-  tree_tiles_kernel<<<S.tiles, kTtAThreads, 0, s>>>(map, codes, S);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_chained(tree_tiles_kernel<OneCloud>, dim3(S.tiles), dim3(kTtAThreads), 0,
+                                 s, map, codes, S);
   if (e != cudaSuccess) return e;
   const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
-  tree_nodes_kernel<<<S.tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
-  return cudaGetLastError();
+  return launch_chained(tree_nodes_kernel<OneCloud>, dim3(S.tiles), dim3(kTtBThreads), 0, s, map,
+                        codes, S, o);
 }
 
 cudaError_t launch_batch_radix_tree(const int4* tiles, int n_tiles, const int* start,
@@ -818,12 +820,12 @@ cudaError_t launch_batch_radix_tree(const int4* tiles, int n_tiles, const int* s
   if (n_tiles <= 0) return cudaSuccess;
   const TreeScratch S = tree_scratch_carve_tiles(scratch, n_tiles);
   const CloudTiles map{tiles, start, unique_c};
-  tree_tiles_kernel<<<n_tiles, kTtAThreads, 0, s>>>(map, codes, S);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_chained(tree_tiles_kernel<CloudTiles>, dim3(n_tiles), dim3(kTtAThreads), 0,
+                                 s, map, codes, S);
   if (e != cudaSuccess) return e;
   const TreeOut o{prefix_n, hll, hlr, left_child, parent, ec};
-  tree_nodes_kernel<<<n_tiles, kTtBThreads, 0, s>>>(map, codes, S, o);
-  return cudaGetLastError();
+  return launch_chained(tree_nodes_kernel<CloudTiles>, dim3(n_tiles), dim3(kTtBThreads), 0, s, map,
+                        codes, S, o);
 }
 
 }  // namespace octgb
