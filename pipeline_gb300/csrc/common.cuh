@@ -24,8 +24,8 @@ constexpr uint32_t kWaitPollCap = 1u << 26;
 constexpr int kWarp = 32;
 
 // Programmatic dependent launch. A kernel launched by launch_chained (host
-// side, kernels.cuh) may have its CTAs scheduled while the kernel before it
-// on the stream is still finishing; chain_wait() blocks until that kernel has
+// side, kernels.cuh) into a CUDA graph may have its CTAs scheduled while the
+// kernel before it is still finishing; chain_wait() blocks until that kernel has
 // completed and its writes are visible (for a kernel launched without the
 // attribute it returns at once). Every kernel that launch_chained launches
 // calls chain_wait() before its first global-memory access, then

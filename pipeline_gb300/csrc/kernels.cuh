@@ -32,15 +32,29 @@ static inline void mark(Recorder* r, cudaStream_t s) {
 // SM count of the current device (cached per device).
 int device_sm_count();
 
-// Whether launch_chained sets the programmatic-serialization attribute: on
-// unless the environment sets OCT_PDL=0 (read once per process).
+// Whether launch_chained may set the programmatic-serialization attribute:
+// yes unless the environment sets OCT_PDL=0 (read once per process).
 bool chained_launches();
 
-// Launch of a kernel whose body starts with chain_enter() (common.cuh), with
-// programmatic stream serialization: its CTAs may be scheduled during the
-// tail of the previous kernel on the stream and wait there on the device, so
-// consecutive kernels (and their CUDA-graph replays) do not pay a full launch
-// gap. Results are the same as a plain launch's.
+// True while `s` is being captured into a CUDA graph (a failed query, e.g.
+// on the legacy stream during another thread's global capture, counts as
+// not capturing and its error is cleared).
+static inline bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return cs == cudaStreamCaptureStatusActive;
+}
+
+// Launch of a kernel whose body starts with chain_enter() (common.cuh). While
+// the stream is captured into a CUDA graph the launch carries programmatic
+// stream serialization, so in the graph's replays the kernel's CTAs may be
+// scheduled during the tail of the kernel before it and wait there on the
+// device, without a full launch gap between them; launched directly on a
+// stream (timed builds, pipelines overlapping copies on other streams) it is
+// a plain launch. Results are the same either way.
 template <typename... P, typename... A>
 static inline cudaError_t launch_chained(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
                                          cudaStream_t s, A&&... args) {
@@ -53,7 +67,7 @@ static inline cudaError_t launch_chained(void (*kernel)(P...), dim3 grid, dim3 b
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   c.attrs = at;
-  c.numAttrs = chained_launches() ? 1 : 0;
+  c.numAttrs = chained_launches() && stream_capturing(s) ? 1 : 0;
   return cudaLaunchKernelEx(&c, kernel, static_cast<P>(args)...);
 }
 
