@@ -188,10 +188,15 @@ def cpu_baseline(pts, reps=2):
     threads = O.lib().orc_max_threads()
     times, _ = cpu_build_time(pts, threads, reps)
     t = statistics.median(times)
+    # the same CPU path on one thread (the reference run with OMP_NUM_THREADS=1)
+    (t1,), _ = cpu_build_time(pts, 1, 1)
     return {"value": len(pts) / t / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{reps} whole builds of the 16,777,216-point cloud, median "
+            "sample": f"{reps} whole builds of the {len(pts):,}-point cloud, median "
                       f"{t * 1e3:.0f} ms each (stages 1-8; octree stage multi-threaded as in the "
-                      f"reference)"}
+                      f"reference)",
+            "single_thread": {"value": len(pts) / t1 / 1e6, "unit": UNIT, "cores": 1,
+                              "sample": f"1 whole build of the same cloud on one thread, "
+                                        f"{t1 * 1e3:.0f} ms"}}
 
 
 def run_reference(args, rank, world):
