@@ -186,17 +186,29 @@ def cpu_baseline(pts, reps=2):
     from oracle import oracle as O
 
     threads = O.lib().orc_max_threads()
-    times, _ = cpu_build_time(pts, threads, reps)
+    times, r = cpu_build_time(pts, threads, reps)
     t = statistics.median(times)
     # the same CPU path on one thread (the reference run with OMP_NUM_THREADS=1)
-    (t1,), _ = cpu_build_time(pts, 1, 1)
+    (t1,), r1 = cpu_build_time(pts, 1, 1)
     return {"value": len(pts) / t / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{reps} whole builds of the {len(pts):,}-point cloud, median "
                       f"{t * 1e3:.0f} ms each (stages 1-8; octree stage multi-threaded as in the "
                       f"reference)",
+            "stages_ms": cpu_stage_ms(r),
             "single_thread": {"value": len(pts) / t1 / 1e6, "unit": UNIT, "cores": 1,
                               "sample": f"1 whole build of the same cloud on one thread, "
-                                        f"{t1 * 1e3:.0f} ms"}}
+                                        f"{t1 * 1e3:.0f} ms",
+                              "stages_ms": cpu_stage_ms(r1)}}
+
+
+CPU_STAGES = ["morton", "sort", "unique", "radix tree", "edge count", "prefix sum",
+              "make octnodes", "link leaf nodes"]
+
+
+def cpu_stage_ms(r):
+    """Per-stage wall times (ms) of one CPU build (the reference's eight stage
+    calls, kernels/01_morton.cpp ... 07_octree.cpp)."""
+    return {k: round(float(v), 2) for k, v in zip(CPU_STAGES, r["stage_ms"])}
 
 
 def run_reference(args, rank, world):
