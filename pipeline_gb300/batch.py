@@ -43,10 +43,21 @@ def pack_shard(points, mins, ranges, sizes, clouds):
     """The listed clouds' points packed one after another, and their mins and
     ranges. `points` is the whole batch's (N x 4) float32 tensor or a list of
     per-cloud arrays; `mins` and `ranges` hold one value per cloud of the
-    batch. Runs on whichever device the inputs are on."""
+    batch. Runs on whichever device the inputs are on. Raises ValueError
+    when the points do not hold the sizes' rows of 4 values."""
     if isinstance(points, (list, tuple)):
+        if len(points) != len(sizes):
+            raise ValueError("one array of points per cloud of the batch")
         parts = [torch.as_tensor(points[c]) for c in clouds]
+        for c, part in zip(clouds, parts):
+            if tuple(part.shape) != (int(sizes[c]), 4):
+                raise ValueError(f"cloud {c}: points of shape {tuple(part.shape)}, "
+                                 f"expected ({int(sizes[c])}, 4)")
     else:
+        points = torch.as_tensor(points)
+        total = int(np.sum(np.asarray(sizes, np.int64)))
+        if points.dim() != 2 or points.shape[1] != 4 or points.shape[0] < total:
+            raise ValueError(f"points of shape {tuple(points.shape)}: expected ({total}, 4)")
         parts = [points[lo:hi] for lo, hi in shard_slices(sizes, clouds)]
     mins = torch.as_tensor(mins, dtype=torch.float32)
     ranges = torch.as_tensor(ranges, dtype=torch.float32)

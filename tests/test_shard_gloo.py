@@ -160,3 +160,26 @@ def test_rank_without_clouds_builds_nothing():
         ShardBuilder([5, 7], 3, 3, device="cpu")
     with pytest.raises(ValueError):
         ShardBuilder([5, 7], 0, 0, device="cpu")
+
+
+def test_pack_shard_rejects_points_that_do_not_match_the_sizes():
+    import pytest
+
+    from pipeline_gb300.batch import pack_shard
+
+    sizes = [3, 2]
+    good = [np.zeros((3, 4), np.float32), np.ones((2, 4), np.float32)]
+    pts, mn, rg = pack_shard(good, [0.0, 1.0], [8.0, 9.0], sizes, [1])
+    assert pts.shape == (2, 4) and float(pts.sum()) == 8.0
+    assert mn.tolist() == [1.0] and rg.tolist() == [9.0]
+    with pytest.raises(ValueError):
+        pack_shard([good[0], np.ones((3, 4), np.float32)], [0.0, 1.0], [8.0, 9.0], sizes, [1])
+    with pytest.raises(ValueError):
+        pack_shard(good[:1], [0.0], [8.0], sizes, [0])
+    with pytest.raises(ValueError):
+        pack_shard(torch.zeros((4, 4)), [0.0, 1.0], [8.0, 9.0], sizes, [0])
+    with pytest.raises(ValueError):
+        pack_shard(torch.zeros((5, 3)), [0.0, 1.0], [8.0, 9.0], sizes, [0])
+    whole = np.arange(20, dtype=np.float32).reshape(5, 4)  # a numpy batch packs like a tensor
+    pts, _, _ = pack_shard(whole, [0.0, 1.0], [8.0, 9.0], sizes, [1, 0])
+    assert pts[:, 0].tolist() == [12.0, 16.0, 0.0, 4.0, 8.0]
