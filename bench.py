@@ -174,7 +174,7 @@ def cpu_build_time(pts, threads, reps):
     """Seconds per whole CPU build (stages 1-8, OpenMP as the reference)."""
     from oracle import oracle as O
 
-    times = []
+    times, r = [], None
     for _ in range(reps):
         r = O.build_all(pts, MIN_COORD, RANGE, threads=threads, parallel_octree=threads > 1,
                         keep_morton=False)
